@@ -1,0 +1,257 @@
+"""Benchmark: MR-LBM D3Q27 throughput (MLUPS) and HBM roofline on the 256^3 Taylor-Green
+vortex (periodic, u0 = 0.05, Re = 1600), the workload the headline metric is quoted on.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--storage f32|f16|bf16] [--impl ours|reference]
+
+One step = one full time step of the solver (stream + collide, one fused kernel) over the
+256^3 grid.  `value` is device-timed with inputs resident in HBM; `e2e` goes through the C
+ABI with host buffers: the initial moment field is uploaded from pinned memory, every step
+reads back its FP64 mass / energy sample, and the final field is read back, all inside the
+timed region.  The reference arm (--impl reference) times the CPU restatement of the
+reference algorithm (the reference has no CPU path) on a bounded slab of the same workload.
+Multi-GPU: the path does not shard across GPUs in this build, so N > 1 runs N independent
+replicas (weak scaling), one per rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+B_ALG = {"f32": 152.0, "f16": 76.0, "bf16": 76.0}   # algorithmic bytes per lattice update
+B_MIN = {"f32": 80.0, "f16": 40.0, "bf16": 40.0}    # moments in + out only
+STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (OSError, FileNotFoundError):
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_baseline(n: int, slab: int, steps: int, bits: int = 32):
+    """Oracle (CPU restatement of the reference step) on an n x n x slab piece of the TGV."""
+    import oracle
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    desc = cases.periodic_box(n, n, slab, u0=0.05, re=1600.0, length=n / (2 * math.pi))
+    o = oracle.Oracle(desc, bits)
+    o.init(N.INIT_TAYLOR_GREEN, (0.05, n / (2 * math.pi)))
+    o.step(1)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    cores = os.cpu_count() or 1
+    return {"value": n * n * slab * steps / dt / 1e6, "unit": "MLUPS", "cores": cores, "kind": "port",
+            "sample": f"{steps} steps of a {n}x{n}x{slab} periodic slab of the same Taylor-Green field, "
+                      f"FP{bits} restatement, OpenMP {cores} threads"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    n = args.n
+    slab = max(4, args.ref_slab)
+    res = None
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(n, slab, 1)
+    for _ in range(args.steps):
+        res = cpu_baseline(n, slab, 1)
+        vals.append(res["value"])
+    value = float(np.median(vals)) if vals else 0.0
+    line = {
+        "impl": "reference", "metric": "MLUPS (D3Q27 MR-LBM, 256^3 Taylor-Green)", "value": value, "unit": "MLUPS",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"taylor-green {n}^3 D3Q27, u0=0.05, Re=1600", "storage": "f32"},
+        "cpu_baseline": {**res, "value": value} if res else None,
+        "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    from mrlbm_3d_cuda_gb300 import native as N
+
+    storage = args.storage
+    desc = cases.c2_taylor_green(args.n, STORAGE[storage])
+    n_nodes = desc.nx * desc.ny * desc.nz
+    stream = torch.cuda.current_stream()
+    sim = Simulation(desc, init=False)
+    sim.set_stream(stream.cuda_stream)
+    sim.init(N.INIT_TAYLOR_GREEN, cases.tgv_params(desc))
+    info = sim.get_info()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident timing --------------------------------------------------------
+    sim.step(args.warmup)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0.record(stream)
+        sim.step(args.steps)
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * n_nodes * args.steps / (ms * 1e-3) / 1e6
+    kernel_ms = ms_step  # one step-kernel launch per step, back to back on one stream
+
+    # ---- end-to-end through the C ABI with host buffers -----------------------------------
+    host = torch.empty((10, n_nodes), dtype=torch.float32, pin_memory=True)
+    hv = host.numpy()
+    sim.moments(out=hv)  # current state as the e2e input
+    sim.set_sampling(0, 1)
+    e2e_steps = max(1, args.steps)
+    barrier()
+    t0 = time.perf_counter()
+    sim.set_moments(hv)
+    sim.step(e2e_steps)
+    _, diag = sim.diagnostics(e2e_steps)
+    sim.moments(out=hv)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * n_nodes * e2e_steps / e2e_s / 1e6
+    sim.set_sampling(0, 0)
+    assert np.isfinite(diag).all()
+
+    peak, peak_kind = measured_peaks()
+    achieved = n_nodes * B_ALG[storage] / (kernel_ms * 1e-3) / 1e9
+    line = {
+        "metric": "MLUPS (D3Q27 MR-LBM, 256^3 Taylor-Green)" if args.n == 256 else f"MLUPS (D3Q27 MR-LBM, {args.n}^3 TGV)",
+        "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": storage, "data": "synthetic",
+        "config": {"workload": f"taylor-green {args.n}^3 D3Q27, u0=0.05, Re=1600, {storage} moment storage",
+                   "storage": storage, "tile": list(info.tile), "ctas": int(info.reserved[0]),
+                   "l2": f"inputs larger than L2 ({n_nodes * 10 * (4 if storage == 'f32' else 2) / 1e6:.0f} MB "
+                         f"per moment buffer vs 129 MB L2)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "bytes_per_lup": B_ALG[storage],
+                     "frac_vs_min_traffic": n_nodes * B_MIN[storage] / (kernel_ms * 1e-3) / 1e9 / peak,
+                     "traffic": None},
+        "e2e": {"value": e2e_value, "unit": "MLUPS", "h2d_bytes_per_step": hv.nbytes / e2e_steps,
+                "d2h_bytes_per_step": 16 + hv.nbytes / e2e_steps},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(min(args.n, 128), 8, args.cpu_steps)
+    sim.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--storage", default="f32", choices=list(STORAGE))
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--ref-slab", type=int, default=8)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

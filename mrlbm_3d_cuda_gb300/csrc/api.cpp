@@ -1,0 +1,751 @@
+// Host runtime behind the C ABI of include/mrlbm.h: case setup, device memory, the time
+// loop, sampling and host-facing I/O.  One handle = one case on the current CUDA device,
+// one stream; no call exits the process (the reference's checkCudaErrors does,
+// MRLBM_3D/src/utils/cudaHelpers.cuh:10-21).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "lattice_tables.h"
+#include "mrlbm_internal.h"
+
+using namespace mrlbm;
+
+namespace {
+thread_local std::string g_last_error;
+constexpr int kRing = 65536;  // sampled steps kept on the device (forces, diagnostics)
+}  // namespace
+
+struct mrlbm_handle {
+    mrlbm_case_desc d{};
+    Derived der{};
+    Geometry geo;
+    std::string err;
+    bool host_only = false;
+    int dev = 0, n_sm = 0;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    int storage = 0, vbytes = 4;
+    StorageScale sc{};
+    int64_t n = 0, fs = 0;
+    void *m[2] = {nullptr, nullptr};
+    int parity = 0;
+    bool initialized = false;
+    int64_t step = 0;
+    // step-kernel configuration
+    int tile_y = 8, lz = 32, tiles_x = 0, tiles_y = 0, n_items = 0, n_ctas = 0;
+    int64_t n_fluid = 0;
+    uint32_t *d_word = nullptr;
+    int32_t *d_items = nullptr, *d_tile_slot = nullptr;
+    float *d_side = nullptr;
+    int n_special = 0;
+    // walls
+    float *d_wf[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    uint32_t *d_wm[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    int64_t *d_wl[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    uint32_t *d_tag = nullptr;  // [512]: in masks then out masks
+    StepArgs args{};
+    StepArgs *d_args = nullptr;
+    int *d_error = nullptr;
+    // sampling
+    int force_every = 0, diag_every = 0;
+    double *d_force_ring = nullptr, *d_diag_ring = nullptr, *d_diag_part = nullptr;
+    std::vector<int64_t> force_steps, diag_steps;
+    int64_t force_count = 0, diag_count = 0;
+    // staging
+    float *d_stage = nullptr;
+    size_t stage_bytes = 0;
+};
+
+namespace {
+
+int fail(mrlbm_handle *h, int code, const std::string &msg) {
+    if (h) h->err = msg;
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(mrlbm_handle *h, cudaError_t e, const char *what) {
+    const int code = (e == cudaErrorMemoryAllocation) ? MRLBM_ERR_NOMEM
+                     : (e == cudaErrorNoKernelImageForDevice || e == cudaErrorUnsupportedPtxVersion) ? MRLBM_ERR_UNSUPPORTED
+                                                                                                      : MRLBM_ERR_CUDA;
+    return fail(h, code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(h, call)                                         \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+    } while (0)
+
+template <typename T>
+cudaError_t upload(T **dptr, const T *host, size_t count) {
+    if (count == 0) {
+        *dptr = nullptr;
+        return cudaSuccess;
+    }
+    cudaError_t e = cudaMalloc((void **)dptr, count * sizeof(T));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*dptr, host, count * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+void free_all(mrlbm_handle *h) {
+    auto f = [](void *p) {
+        if (p) cudaFree(p);
+    };
+    f(h->m[0]);
+    f(h->m[1]);
+    f(h->d_word);
+    f(h->d_items);
+    f(h->d_tile_slot);
+    f(h->d_side);
+    for (int w = 0; w < 2; ++w) {
+        for (int k = 0; k < 3; ++k) f(h->d_wf[w][k]);
+        for (int k = 0; k < 2; ++k) f(h->d_wm[w][k]);
+        for (int k = 0; k < 2; ++k) f(h->d_wl[w][k]);
+    }
+    f(h->d_tag);
+    f(h->d_args);
+    f(h->d_error);
+    f(h->d_force_ring);
+    f(h->d_diag_ring);
+    f(h->d_diag_part);
+    f(h->d_stage);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+int64_t node_index_for_layout(const mrlbm_handle *h, int64_t lex, int layout) {
+    if (layout != MRLBM_LAYOUT_REF_TILED) return lex;
+    const int nx = h->d.nx, ny = h->d.ny;
+    const int x = (int)(lex % nx), y = (int)((lex / nx) % ny), z = (int)(lex / ((int64_t)nx * ny));
+    return ref_tiled_index(x, y, z, nx, ny);
+}
+
+int ensure_stage(mrlbm_handle *h, size_t bytes) {
+    if (h->stage_bytes >= bytes) return MRLBM_OK;
+    if (h->d_stage) cudaFree(h->d_stage);
+    h->d_stage = nullptr;
+    h->stage_bytes = 0;
+    CK(h, cudaMalloc((void **)&h->d_stage, bytes));
+    h->stage_bytes = bytes;
+    return MRLBM_OK;
+}
+
+int choose_tiling(mrlbm_handle *h) {
+    const char *ety = std::getenv("MRLBM_TILE_Y");
+    const char *elz = std::getenv("MRLBM_LZ");
+    int ty = ety ? std::atoi(ety) : 8;
+    if (ty != 4 && ty != 8 && ty != 16) ty = 8;
+    h->tile_y = ty;
+    h->tiles_x = (h->d.nx + TILE_X - 1) / TILE_X;
+    h->tiles_y = (h->d.ny + ty - 1) / ty;
+    int per_sm = step_kernel_max_ctas_per_sm(h->storage, ty);
+    if (per_sm <= 0) per_sm = 1;
+    const int resident = per_sm * h->n_sm;
+    const int tiles = h->tiles_x * h->tiles_y;
+    int lz = h->d.nz;
+    if (elz) {
+        lz = std::max(1, std::min(h->d.nz, std::atoi(elz)));
+    } else {
+        // longest z-segment that still gives every resident CTA several work items
+        while (lz > 16 && (int64_t)tiles * ((h->d.nz + lz - 1) / lz) < 4LL * resident) lz = (lz + 1) / 2;
+    }
+    h->lz = lz;
+    return resident;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mrlbm_abi_version(void) { return MRLBM_ABI_VERSION; }
+
+const char *mrlbm_last_error(const mrlbm_handle *h) { return h ? h->err.c_str() : g_last_error.c_str(); }
+
+int mrlbm_case_desc_default(mrlbm_case_desc *d, int32_t geometry) {
+    if (!d) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null descriptor");
+    std::memset(d, 0, sizeof(*d));
+    d->struct_size = sizeof(*d);
+    d->geometry = geometry;
+    d->rho0 = 1.0f;
+    d->triangular = 1;
+    d->mass_bc = MRLBM_MASS_EQUILIBRIUM;
+    d->bcf_mass_bc = MRLBM_MASS_EQUILIBRIUM;
+    d->storage = MRLBM_STORAGE_F32;
+    if (geometry == MRLBM_GEOM_CYLINDER) {
+        // MRLBM_3D/src/cases/cylinder/constants.cuh:8-54
+        const int D = 16, LW = 4 * D, LE = 16 * D, LN = 4 * D, LS = LN;
+        d->nx = LW + D + LE;
+        d->ny = LN + D + LS;
+        d->nz = 3 * D;
+        d->periodic[0] = 0;
+        d->periodic[1] = 1;
+        d->periodic[2] = 1;
+        d->convective_outlet = 1;
+        d->u_max = 0.1f;
+        d->re = 100.0f;
+        d->d_wall[0] = (float)D;
+        d->xc = (float)(LW + 0.5 * (D - 1));
+        d->yc = (float)(LS + 0.5 * (D - 1));
+        d->scan_box[0] = LW - 4;
+        d->scan_box[1] = LW + D + 4;
+        d->scan_box[2] = LS - 4;
+        d->scan_box[3] = LS + D + 4;
+    } else if (geometry == MRLBM_GEOM_ANNULUS) {
+        // MRLBM_3D/src/cases/annulus/constants.cuh:19-84
+        const float d_out = 128.0f, r_out = 0.5f * d_out, r_in = 0.5f * r_out;
+        d->nx = 136;
+        d->ny = 136;
+        d->nz = 256;
+        d->periodic[0] = 0;
+        d->periodic[1] = 0;
+        d->periodic[2] = 1;
+        d->u_max = 0.03f;
+        d->re = 70.0f;
+        d->d_wall[0] = 2.0f * r_in;
+        d->d_wall[1] = d_out;
+        d->xc = (float)(0.5 * (136 - 1));
+        d->yc = (float)(0.5 * (136 - 1));
+        const float vel_scale = d->u_max / r_in;
+        d->wall_u[0][1] = vel_scale * r_in;
+        d->scan_box[0] = 0;
+        d->scan_box[1] = d->nx;
+        d->scan_box[2] = 0;
+        d->scan_box[3] = d->ny;
+    } else if (geometry == MRLBM_GEOM_NONE) {
+        d->nx = d->ny = d->nz = 64;
+        d->periodic[0] = d->periodic[1] = d->periodic[2] = 1;
+        d->u_max = 0.05f;
+        d->re = 1600.0f;
+        d->length = (float)(64.0 / (2.0 * M_PI));
+    } else {
+        return fail(nullptr, MRLBM_ERR_INVALID_ARG, "unknown geometry");
+    }
+    return MRLBM_OK;
+}
+
+int mrlbm_case_desc_finalize(mrlbm_case_desc *d) {
+    if (!d || d->struct_size != sizeof(*d)) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "descriptor size mismatch");
+    if (d->nx <= 0 || d->ny <= 0 || d->nz <= 0 || d->nx % 8 || d->ny % 8 || d->nz % 4)
+        return fail(nullptr, MRLBM_ERR_INVALID_ARG, "grid must be positive multiples of 8 x 8 x 4");
+    if (d->nx < 8 || d->ny < 8 || d->nz < 4) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "grid too small");
+    if ((int64_t)d->nx * d->ny * d->nz >= (1LL << 31) * 8)
+        return fail(nullptr, MRLBM_ERR_INVALID_ARG, "grid too large");
+    if (d->storage < 0 || d->storage > 2) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "bad storage");
+    if (d->geometry < 0 || d->geometry > 2) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "bad geometry");
+    if (d->neumann_current_update)
+        return fail(nullptr, MRLBM_ERR_UNSUPPORTED, "NEUMANN_CURRENT_UPDATE outlet is not built");
+    if (!(d->rho0 > 0.f)) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "rho0 must be positive");
+    if (d->omega <= 0.f && !(d->re > 0.f)) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "need re > 0 or omega > 0");
+    if (d->geometry == MRLBM_GEOM_NONE && d->omega <= 0.f && !(d->length > 0.f))
+        return fail(nullptr, MRLBM_ERR_INVALID_ARG, "need length > 0 to derive omega");
+    if (d->geometry == MRLBM_GEOM_ANNULUS && !(d->d_wall[1] > d->d_wall[0]))
+        return fail(nullptr, MRLBM_ERR_INVALID_ARG, "annulus needs d_wall[1] > d_wall[0]");
+    Derived der;
+    const std::string e = derive(*d, der);
+    if (!e.empty()) return fail(nullptr, MRLBM_ERR_INVALID_ARG, e);
+    return MRLBM_OK;
+}
+
+int mrlbm_create_host(const mrlbm_case_desc *din, mrlbm_handle **out) {
+    if (!din || !out) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    mrlbm_case_desc d = *din;
+    int rc = mrlbm_case_desc_finalize(&d);
+    if (rc) return rc;
+    std::unique_ptr<mrlbm_handle> h(new mrlbm_handle());
+    h->d = d;
+    derive(h->d, h->der);
+    const std::string ge = classify(h->d, h->geo);
+    if (!ge.empty()) return fail(nullptr, MRLBM_ERR_INVALID_ARG, ge);
+    h->n = (int64_t)d.nx * d.ny * d.nz;
+    h->storage = d.storage;
+    h->vbytes = d.storage == MRLBM_STORAGE_F32 ? 4 : 2;
+    h->host_only = true;
+    *out = h.release();
+    return MRLBM_OK;
+}
+
+int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
+    if (!din || !out) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    mrlbm_case_desc d = *din;
+    int rc = mrlbm_case_desc_finalize(&d);
+    if (rc) return rc;
+    std::unique_ptr<mrlbm_handle> h(new mrlbm_handle());
+    h->d = d;
+    derive(h->d, h->der);
+    CK(h.get(), cudaGetDevice(&h->dev));
+    CK(h.get(), cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, h->dev));
+    int major = 0, minor = 0;
+    CK(h.get(), cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, h->dev));
+    CK(h.get(), cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, h->dev));
+    if (!(major == 10 && minor == 3)) {
+        fail(nullptr, MRLBM_ERR_UNSUPPORTED, "libmrlbm is built for sm_103a (GB300) only");
+        return MRLBM_ERR_UNSUPPORTED;
+    }
+    CK(h.get(), cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
+    h->stream = h->own_stream;
+
+    // geometry on the host
+    const std::string ge = classify(h->d, h->geo);
+    if (!ge.empty()) {
+        const std::string msg = ge;
+        free_all(h.get());
+        return fail(nullptr, MRLBM_ERR_INVALID_ARG, msg);
+    }
+    const Geometry &g = h->geo;
+    h->n = (int64_t)d.nx * d.ny * d.nz;
+    h->fs = (h->n + 63) / 64 * 64;  // 256-byte aligned field planes for any storage type
+    h->storage = d.storage;
+    h->vbytes = d.storage == MRLBM_STORAGE_F32 ? 4 : 2;
+    for (int k = 0; k < 3; ++k) {
+        float s = d.storage_scale[k];
+        if (d.storage == MRLBM_STORAGE_F32) s = 1.f;
+        else if (!(s > 0.f)) {
+            const float u = d.u_max > 0.f ? d.u_max : 0.05f;
+            s = k == 1 ? 1.0f / u : 1.0f / (u * u);
+        }
+        h->sc.s[k] = s;
+        h->sc.is[k] = 1.0f / s;
+    }
+
+    // node words, tile classes, work items
+    const int resident = choose_tiling(h.get());
+    const int tiles = h->tiles_x * h->tiles_y;
+    std::vector<uint32_t> word(h->n, 0);
+    bool any_special = false;
+    int64_t n_fluid = 0;
+    for (int64_t i = 0; i < h->n; ++i) {
+        word[i] = make_word(g.cls[i], g.payload[i], g.frozen[i] != 0, g.stencil[i] != 0);
+        if (word[i]) any_special = true;
+        const uint32_t c = g.cls[i];
+        if (!g.frozen[i] && c != C_SOLID && c != C_INNER && c != C_OUTER) ++n_fluid;
+    }
+    h->n_fluid = n_fluid;
+    std::vector<int32_t> slot(tiles, -1);
+    std::vector<char> skip(tiles, 0);
+    int n_special = 0;
+    for (int t = 0; t < tiles; ++t) {
+        const int x0 = (t % h->tiles_x) * TILE_X, y0 = (t / h->tiles_x) * h->tile_y;
+        bool special = false, all_frozen = true;
+        for (int z = 0; z < d.nz; ++z)
+            for (int y = y0; y < std::min(d.ny, y0 + h->tile_y); ++y)
+                for (int x = x0; x < std::min(d.nx, x0 + TILE_X); ++x) {
+                    const int64_t i = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
+                    if (word[i]) special = true;
+                    if (!g.frozen[i]) all_frozen = false;
+                }
+        if (all_frozen) skip[t] = 1;
+        else if (special) slot[t] = n_special++;
+    }
+    h->n_special = n_special;
+    const int nseg = (d.nz + h->lz - 1) / h->lz;
+    std::vector<int32_t> items;
+    for (int s = 0; s < nseg; ++s)
+        for (int t = 0; t < tiles; ++t)
+            if (!skip[t]) items.push_back(t | (s << 20));
+    h->n_items = (int)items.size();
+    h->n_ctas = std::max(1, std::min(h->n_items, resident));
+
+    mrlbm_handle *H = h.get();
+    const size_t mbytes = (size_t)h->fs * 10 * h->vbytes;
+    CK(H, cudaMalloc(&h->m[0], mbytes));
+    CK(H, cudaMalloc(&h->m[1], mbytes));
+    CK(H, cudaMemset(h->m[0], 0, mbytes));
+    CK(H, cudaMemset(h->m[1], 0, mbytes));
+    if (any_special) {
+        CK(H, upload(&h->d_word, word.data(), word.size()));
+        CK(H, upload(&h->d_tile_slot, slot.data(), slot.size()));
+        if (n_special > 0) {
+            const size_t side_floats = (size_t)n_special * d.nz * TILE_X * h->tile_y * 16;
+            CK(H, cudaMalloc((void **)&h->d_side, side_floats * sizeof(float)));
+            CK(H, cudaMemset(h->d_side, 0, side_floats * sizeof(float)));
+        }
+    }
+    CK(H, upload(&h->d_items, items.data(), items.size()));
+    for (int w = 0; w < g.n_walls; ++w) {
+        const WallData &wd = g.wall[w];
+        CK(H, upload(&h->d_wf[w][0], wd.nx.data(), wd.nx.size()));
+        CK(H, upload(&h->d_wf[w][1], wd.ny.data(), wd.ny.size()));
+        CK(H, upload(&h->d_wf[w][2], wd.delta.data(), wd.delta.size()));
+        CK(H, upload(&h->d_wm[w][0], wd.in_mask.data(), wd.in_mask.size()));
+        CK(H, upload(&h->d_wm[w][1], wd.out_mask.data(), wd.out_mask.size()));
+        CK(H, upload(&h->d_wl[w][0], wd.list.data(), wd.list.size()));
+        CK(H, upload(&h->d_wl[w][1], wd.fluid_list.data(), wd.fluid_list.size()));
+    }
+    {
+        std::vector<uint32_t> tags(512);
+        std::memcpy(tags.data(), g.tag_in_mask, 256 * 4);
+        std::memcpy(tags.data() + 256, g.tag_out_mask, 256 * 4);
+        CK(H, upload(&h->d_tag, tags.data(), tags.size()));
+    }
+    CK(H, cudaMalloc((void **)&h->d_error, sizeof(int)));
+    CK(H, cudaMemset(h->d_error, 0, sizeof(int)));
+    CK(H, cudaMalloc((void **)&h->d_force_ring, (size_t)kRing * 10 * sizeof(double)));
+    CK(H, cudaMalloc((void **)&h->d_diag_ring, (size_t)kRing * 2 * sizeof(double)));
+    CK(H, cudaMalloc((void **)&h->d_diag_part, (size_t)h->n_ctas * 2 * sizeof(double)));
+    h->force_steps.assign(kRing, -1);
+    h->diag_steps.assign(kRing, -1);
+
+    StepArgs &a = h->args;
+    a.m[0] = h->m[0];
+    a.m[1] = h->m[1];
+    a.fs = h->fs;
+    a.word = h->d_word;
+    a.items = h->d_items;
+    a.n_items = h->n_items;
+    a.tile_slot = h->d_tile_slot;
+    a.side = h->d_side;
+    a.nx = d.nx;
+    a.ny = d.ny;
+    a.nz = d.nz;
+    a.tiles_x = h->tiles_x;
+    a.tiles_y = h->tiles_y;
+    a.tile_y = h->tile_y;
+    a.lz = h->lz;
+    a.omega = h->der.omega;
+    a.rho0 = d.rho0;
+    a.u_max = d.u_max;
+    a.convective = d.convective_outlet;
+    a.current_update = d.neumann_current_update;
+    a.bcf_strong = d.bcf_mass_bc == MRLBM_MASS_STRONG;
+    a.wall_strong = d.mass_bc == MRLBM_MASS_STRONG;
+    a.xc = d.xc;
+    a.yc = d.yc;
+    a.sc = h->sc;
+    for (int w = 0; w < g.n_walls; ++w) {
+        WallArgs &W = a.wall[w];
+        W.nx = h->d_wf[w][0];
+        W.ny = h->d_wf[w][1];
+        W.delta = h->d_wf[w][2];
+        W.in_mask = h->d_wm[w][0];
+        W.out_mask = h->d_wm[w][1];
+        W.list = h->d_wl[w][0];
+        W.fluid_list = h->d_wl[w][1];
+        W.nb = (int)g.wall[w].list.size();
+        W.nbf = (int)g.wall[w].fluid_list.size();
+        W.r_wall = 0.5f * d.d_wall[w];
+        W.dir = w == 1 ? -1.0f : 1.0f;
+        for (int k = 0; k < 3; ++k) W.u_wall[k] = d.wall_u[w][k];
+    }
+    a.tag_in = h->d_tag;
+    a.tag_out = h->d_tag ? h->d_tag + 256 : nullptr;
+    a.error = h->d_error;
+    CK(H, upload(&h->d_args, &a, 1));
+    CK(H, cudaDeviceSynchronize());
+    *out = h.release();
+    return MRLBM_OK;
+}
+
+int mrlbm_destroy(mrlbm_handle *h) {
+    if (!h) return MRLBM_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (!h->host_only) free_all(h);
+    delete h;
+    return MRLBM_OK;
+}
+
+int mrlbm_set_stream(mrlbm_handle *h, void *cuda_stream) {
+    if (!h) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null handle");
+    if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->stream = cuda_stream ? (cudaStream_t)cuda_stream : h->own_stream;
+    return MRLBM_OK;
+}
+
+int mrlbm_get_info(const mrlbm_handle *h, mrlbm_info *info) {
+    if (!h || !info) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null argument");
+    std::memset(info, 0, sizeof(*info));
+    info->nx = h->d.nx;
+    info->ny = h->d.ny;
+    info->nz = h->d.nz;
+    info->n_nodes = h->n;
+    for (int w = 0; w < 2; ++w) {
+        info->nb[w] = (int32_t)h->geo.wall[w].list.size();
+        info->nb_fluid[w] = (int32_t)h->geo.wall[w].fluid_list.size();
+    }
+    info->omega = h->der.omega;
+    info->tau = h->der.tau;
+    info->step = h->step;
+    info->storage = h->storage;
+    info->bytes_per_value = h->vbytes;
+    info->n_active_items = h->n_items;
+    info->tile[0] = TILE_X;
+    info->tile[1] = h->tile_y;
+    info->tile[2] = h->lz;
+    info->reserved[0] = h->n_ctas;
+    info->reserved[1] = h->n_special;
+    info->reserved[2] = (int32_t)std::min<int64_t>(h->n_fluid, INT32_MAX);
+    return MRLBM_OK;
+}
+
+int mrlbm_init(mrlbm_handle *h, int32_t kind, const double *params, int32_t n_params) {
+    if (!h) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null handle");
+    if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    if (kind < 0 || kind > MRLBM_INIT_NOISY_UNIFORM) return fail(h, MRLBM_ERR_INVALID_ARG, "bad init kind");
+    InitArgs ia;
+    ia.m_a = h->m[0];
+    ia.m_b = h->m[1];
+    ia.fs = h->fs;
+    ia.nx = h->d.nx;
+    ia.ny = h->d.ny;
+    ia.nz = h->d.nz;
+    ia.kind = kind;
+    ia.rho0 = h->d.rho0;
+    ia.u_max = h->d.u_max;
+    ia.sc = h->sc;
+    const int need = kind == MRLBM_INIT_TAYLOR_GREEN ? 2 : kind == MRLBM_INIT_UNIFORM ? 3
+                     : kind == MRLBM_INIT_NOISY_UNIFORM ? 5 : 0;
+    if (n_params < need || (need && !params)) return fail(h, MRLBM_ERR_INVALID_ARG, "missing init parameters");
+    for (int k = 0; k < need && k < 8; ++k) ia.p[k] = params[k];
+    CK(h, launch_init(ia, h->storage, h->stream));
+    h->parity = 0;
+    h->step = 0;
+    h->force_count = h->diag_count = 0;
+    std::fill(h->force_steps.begin(), h->force_steps.end(), -1);
+    std::fill(h->diag_steps.begin(), h->diag_steps.end(), -1);
+    h->initialized = true;
+    return MRLBM_OK;
+}
+
+int mrlbm_set_sampling(mrlbm_handle *h, int32_t force_every, int32_t diag_every) {
+    if (!h) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null handle");
+    if (force_every < 0 || diag_every < 0) return fail(h, MRLBM_ERR_INVALID_ARG, "negative sampling period");
+    h->force_every = h->geo.n_walls ? force_every : 0;
+    h->diag_every = diag_every;
+    return MRLBM_OK;
+}
+
+int mrlbm_step(mrlbm_handle *h, int32_t nsteps) {
+    if (!h) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null handle");
+    if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    if (!h->initialized) return fail(h, MRLBM_ERR_STATE, "mrlbm_init / mrlbm_set_moments must come first");
+    if (nsteps < 0) return fail(h, MRLBM_ERR_INVALID_ARG, "negative step count");
+    const int nb = (int)(h->geo.wall[0].list.size() + h->geo.wall[1].list.size());
+    const int nbf = (int)(h->geo.wall[0].fluid_list.size() + h->geo.wall[1].fluid_list.size());
+    for (int s = 0; s < nsteps; ++s) {
+        const int64_t it = h->step;
+        const bool fs = h->force_every > 0 && it % h->force_every == 0;
+        const bool ds = h->diag_every > 0 && it % h->diag_every == 0;
+        StepLaunch L;
+        L.ga = h->d_args;
+        L.parity = h->parity;
+        L.n_ctas = h->n_ctas;
+        if (fs) {
+            const int64_t slot = h->force_count % kRing;
+            L.force = h->d_force_ring + slot * 10;
+            CK(h, cudaMemsetAsync(L.force, 0, 10 * sizeof(double), h->stream));
+            h->force_steps[slot] = it;
+            ++h->force_count;
+        }
+        if (ds) L.diag_part = h->d_diag_part;
+        CK(h, launch_step(L, h->storage, h->tile_y, h->stream));
+        if (nb > 0) CK(h, launch_wall(L, h->storage, nb + (fs ? nbf : 0), h->stream));
+        if (ds) {
+            const int64_t slot = h->diag_count % kRing;
+            CK(h, launch_diag_finalize(h->d_diag_part, h->n_ctas, h->d_diag_ring + slot * 2, h->stream));
+            h->diag_steps[slot] = it;
+            ++h->diag_count;
+        }
+        h->parity ^= 1;
+        ++h->step;
+    }
+    return MRLBM_OK;
+}
+
+int mrlbm_sync(mrlbm_handle *h) {
+    if (!h) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null handle");
+    if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    CK(h, cudaStreamSynchronize(h->stream));
+    int e = 0;
+    CK(h, cudaMemcpy(&e, h->d_error, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) return fail(h, MRLBM_ERR_CUDA, "device reported a stencil lookup failure (code " + std::to_string(e) + ")");
+    if (h->diag_count > 0) {
+        double v[2];
+        const int64_t slot = (h->diag_count - 1) % kRing;
+        CK(h, cudaMemcpy(v, h->d_diag_ring + slot * 2, sizeof(v), cudaMemcpyDeviceToHost));
+        if (!std::isfinite(v[0]) || !std::isfinite(v[1]))
+            return fail(h, MRLBM_ERR_DIVERGED, "mass / energy diagnostics are not finite");
+    }
+    return MRLBM_OK;
+}
+
+int mrlbm_get_moments(mrlbm_handle *h, uint32_t mask, int32_t layout, float *host, size_t count) {
+    if (!h || !host) return fail(h, MRLBM_ERR_INVALID_ARG, "null argument");
+    if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    if (!h->initialized) return fail(h, MRLBM_ERR_STATE, "no state yet");
+    mask &= MRLBM_FIELD_ALL;
+    const int nf = __builtin_popcount(mask);
+    if (nf == 0 || count < (size_t)nf * h->n) return fail(h, MRLBM_ERR_INVALID_ARG, "host buffer too small");
+    if (layout != MRLBM_LAYOUT_LEXICOGRAPHIC && layout != MRLBM_LAYOUT_REF_TILED)
+        return fail(h, MRLBM_ERR_INVALID_ARG, "bad layout");
+    const void *src = h->m[h->parity];
+    if (h->storage == MRLBM_STORAGE_F32 && layout == MRLBM_LAYOUT_LEXICOGRAPHIC) {
+        int k = 0;
+        for (int f = 0; f < 10; ++f) {
+            if (!(mask & (1u << f))) continue;
+            CK(h, cudaMemcpyAsync(host + (size_t)k * h->n, (const float *)src + (size_t)f * h->fs, h->n * 4,
+                                  cudaMemcpyDeviceToHost, h->stream));
+            ++k;
+        }
+    } else {
+        int rc = ensure_stage(h, (size_t)nf * h->n * 4);
+        if (rc) return rc;
+        CK(h, launch_convert(src, nullptr, nullptr, h->d_stage, h->fs, mask, layout, h->d.nx, h->d.ny, h->d.nz,
+                             h->storage, h->sc, 0, h->stream));
+        CK(h, cudaMemcpyAsync(host, h->d_stage, (size_t)nf * h->n * 4, cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    return MRLBM_OK;
+}
+
+int mrlbm_set_moments(mrlbm_handle *h, uint32_t mask, int32_t layout, const float *host, size_t count) {
+    if (!h || !host) return fail(h, MRLBM_ERR_INVALID_ARG, "null argument");
+    if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    mask &= MRLBM_FIELD_ALL;
+    const int nf = __builtin_popcount(mask);
+    if (nf == 0 || count < (size_t)nf * h->n) return fail(h, MRLBM_ERR_INVALID_ARG, "host buffer too small");
+    if (!h->initialized && mask != MRLBM_FIELD_ALL)
+        return fail(h, MRLBM_ERR_STATE, "the first mrlbm_set_moments must set every field");
+    if (layout != MRLBM_LAYOUT_LEXICOGRAPHIC && layout != MRLBM_LAYOUT_REF_TILED)
+        return fail(h, MRLBM_ERR_INVALID_ARG, "bad layout");
+    void *cur = h->m[h->parity], *oth = h->m[h->parity ^ 1];
+    if (h->storage == MRLBM_STORAGE_F32 && layout == MRLBM_LAYOUT_LEXICOGRAPHIC) {
+        int k = 0;
+        for (int f = 0; f < 10; ++f) {
+            if (!(mask & (1u << f))) continue;
+            float *dc = (float *)cur + (size_t)f * h->fs, *dn = (float *)oth + (size_t)f * h->fs;
+            CK(h, cudaMemcpyAsync(dc, host + (size_t)k * h->n, h->n * 4, cudaMemcpyHostToDevice, h->stream));
+            CK(h, cudaMemcpyAsync(dn, dc, h->n * 4, cudaMemcpyDeviceToDevice, h->stream));
+            ++k;
+        }
+    } else {
+        int rc = ensure_stage(h, (size_t)nf * h->n * 4);
+        if (rc) return rc;
+        CK(h, cudaMemcpyAsync(h->d_stage, host, (size_t)nf * h->n * 4, cudaMemcpyHostToDevice, h->stream));
+        CK(h, launch_convert(nullptr, cur, oth, h->d_stage, h->fs, mask, layout, h->d.nx, h->d.ny, h->d.nz, h->storage,
+                             h->sc, 1, h->stream));
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->initialized = true;
+    return MRLBM_OK;
+}
+
+int mrlbm_get_node_types(mrlbm_handle *h, int32_t layout, uint32_t *host, size_t count) {
+    if (!h || !host) return fail(h, MRLBM_ERR_INVALID_ARG, "null argument");
+    if (count < (size_t)h->n) return fail(h, MRLBM_ERR_INVALID_ARG, "host buffer too small");
+    for (int64_t i = 0; i < h->n; ++i)
+        host[node_index_for_layout(h, i, layout)] = ((uint32_t)h->geo.cls[i] << 20) | (h->geo.payload[i] & 0xFFFFFu);
+    return MRLBM_OK;
+}
+
+int mrlbm_get_boundary(mrlbm_handle *h, int32_t wall, int32_t what, int32_t layout, void *host, size_t count) {
+    if (!h || !host || wall < 0 || wall > 1) return fail(h, MRLBM_ERR_INVALID_ARG, "bad argument");
+    const WallData &wd = h->geo.wall[wall];
+    auto copy_list = [&](const std::vector<int64_t> &v) -> int {
+        if (count < v.size()) return fail(h, MRLBM_ERR_INVALID_ARG, "host buffer too small");
+        int64_t *o = (int64_t *)host;
+        for (size_t i = 0; i < v.size(); ++i) o[i] = node_index_for_layout(h, v[i], layout);
+        return MRLBM_OK;
+    };
+    auto copy_f = [&](const std::vector<float> &v) -> int {
+        if (count < v.size()) return fail(h, MRLBM_ERR_INVALID_ARG, "host buffer too small");
+        std::memcpy(host, v.data(), v.size() * 4);
+        return MRLBM_OK;
+    };
+    auto copy_u = [&](const uint32_t *v, size_t n) -> int {
+        if (count < n) return fail(h, MRLBM_ERR_INVALID_ARG, "host buffer too small");
+        std::memcpy(host, v, n * 4);
+        return MRLBM_OK;
+    };
+    switch (what) {
+        case MRLBM_BND_LIST: return copy_list(wd.list);
+        case MRLBM_BND_NORMAL_X: return copy_f(wd.nx);
+        case MRLBM_BND_NORMAL_Y: return copy_f(wd.ny);
+        case MRLBM_BND_DELTA: return copy_f(wd.delta);
+        case MRLBM_BND_IN_MASK: return copy_u(wd.in_mask.data(), wd.in_mask.size());
+        case MRLBM_BND_OUT_MASK: return copy_u(wd.out_mask.data(), wd.out_mask.size());
+        case MRLBM_BND_FLUID_LIST: return copy_list(wd.fluid_list);
+        case MRLBM_BND_TAG_IN_MASK: return copy_u(h->geo.tag_in_mask, 256);
+        case MRLBM_BND_TAG_OUT_MASK: return copy_u(h->geo.tag_out_mask, 256);
+        default: return fail(h, MRLBM_ERR_INVALID_ARG, "bad boundary array id");
+    }
+}
+
+int mrlbm_get_forces(mrlbm_handle *h, int64_t step, double out[10]) {
+    if (!h || !out) return fail(h, MRLBM_ERR_INVALID_ARG, "null argument");
+    if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    CK(h, cudaStreamSynchronize(h->stream));
+    const int64_t lo = std::max<int64_t>(0, h->force_count - kRing);
+    for (int64_t c = h->force_count - 1; c >= lo; --c) {
+        const int64_t slot = c % kRing;
+        if (step < 0 || h->force_steps[slot] == step) {
+            CK(h, cudaMemcpy(out, h->d_force_ring + slot * 10, 10 * sizeof(double), cudaMemcpyDeviceToHost));
+            return MRLBM_OK;
+        }
+    }
+    return fail(h, MRLBM_ERR_STATE, "no force sample for that step");
+}
+
+int mrlbm_get_force_history(mrlbm_handle *h, int32_t max_steps, int64_t *steps, double *forces, int32_t *n_out) {
+    if (!h || !n_out || max_steps < 0) return fail(h, MRLBM_ERR_INVALID_ARG, "bad argument");
+    if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    CK(h, cudaStreamSynchronize(h->stream));
+    const int64_t avail = std::min<int64_t>(h->force_count, kRing);
+    const int64_t n = std::min<int64_t>(avail, max_steps);
+    std::vector<double> ring((size_t)kRing * 10);
+    if (n > 0) CK(h, cudaMemcpy(ring.data(), h->d_force_ring, ring.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t c = h->force_count - n + k;
+        const int64_t slot = c % kRing;
+        if (steps) steps[k] = h->force_steps[slot];
+        if (forces) std::memcpy(forces + k * 10, ring.data() + slot * 10, 10 * sizeof(double));
+    }
+    *n_out = (int32_t)n;
+    return MRLBM_OK;
+}
+
+int mrlbm_get_diagnostics(mrlbm_handle *h, int32_t max_steps, int64_t *steps, double *values, int32_t *n_out) {
+    if (!h || !n_out || max_steps < 0) return fail(h, MRLBM_ERR_INVALID_ARG, "bad argument");
+    if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    CK(h, cudaStreamSynchronize(h->stream));
+    const int64_t avail = std::min<int64_t>(h->diag_count, kRing);
+    const int64_t n = std::min<int64_t>(avail, max_steps);
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t c = h->diag_count - n + k;
+        const int64_t slot = c % kRing;
+        double v[2];
+        CK(h, cudaMemcpy(v, h->d_diag_ring + slot * 2, sizeof(v), cudaMemcpyDeviceToHost));
+        if (steps) steps[k] = h->diag_steps[slot];
+        if (values) {
+            values[2 * k + 0] = (double)h->n_fluid * h->d.rho0 + v[0];
+            values[2 * k + 1] = v[1];
+        }
+    }
+    *n_out = (int32_t)n;
+    return MRLBM_OK;
+}
+
+int mrlbm_checkpoint_save(mrlbm_handle *h, const char *path) {
+    (void)path;
+    return fail(h, MRLBM_ERR_UNSUPPORTED, "checkpoint writer not built yet");
+}
+int mrlbm_checkpoint_load(mrlbm_handle *h, const char *path) {
+    (void)path;
+    return fail(h, MRLBM_ERR_UNSUPPORTED, "checkpoint reader not built yet");
+}
+int mrlbm_write_vti(mrlbm_handle *h, const char *path) {
+    (void)path;
+    return fail(h, MRLBM_ERR_UNSUPPORTED, "vti writer not built yet");
+}
+
+}  // extern "C"

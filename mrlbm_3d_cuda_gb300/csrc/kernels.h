@@ -1,0 +1,90 @@
+// Launch interface between the host runtime (api.cpp) and the CUDA kernels.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace mrlbm {
+
+// Low-precision storage keeps scaled deviations from the rest state: stored = value * scale,
+// one scale for rho - rho0, one for u, one for m.
+struct StorageScale {
+    float s[3];   // multiply on store
+    float is[3];  // multiply on load
+};
+
+struct WallArgs {
+    const float *nx = nullptr, *ny = nullptr, *delta = nullptr;
+    const uint32_t *in_mask = nullptr, *out_mask = nullptr;
+    const int64_t *list = nullptr;  // lexicographic node index
+    const int64_t *fluid_list = nullptr;  // BCFLUID nodes of this wall
+    int nb = 0, nbf = 0;
+    float r_wall = 0.f;             // 0.5 D of the wall
+    float dir = 1.f;                // +1 inner wall (fluid outside), -1 outer wall
+    float u_wall[3] = {0.f, 0.f, 0.f};
+};
+
+// One copy lives in device memory per handle; kernels receive a pointer to it plus the
+// per-step scalars (ping-pong parity, sampling buffers).
+struct StepArgs {
+    void *m[2] = {nullptr, nullptr};  // ping-pong moment buffers, 10 fields, field stride `fs`
+    int64_t fs = 0;
+    const uint32_t *word = nullptr;     // internal node words (lexicographic); null if all bulk
+    const int32_t *items = nullptr;     // work items: tile index | (z-segment << 20)
+    int n_items = 0;
+    const int32_t *tile_slot = nullptr; // per xy tile: -1 plain, >= 0 side-buffer slot
+    float *side = nullptr;              // post-stream moments of stencil nodes, 10 floats each
+    int nx = 0, ny = 0, nz = 0;
+    int tiles_x = 0, tiles_y = 0, tile_y = 8, lz = 32;
+    float omega = 1.f, rho0 = 1.f, u_max = 0.f;
+    int convective = 0, current_update = 0, bcf_strong = 0, wall_strong = 0;
+    float xc = 0.f, yc = 0.f;
+    StorageScale sc;
+    WallArgs wall[2];
+    const uint32_t *tag_in = nullptr, *tag_out = nullptr;  // [256] BCFLUID masks
+    int *error = nullptr;     // sticky device error flag
+};
+
+// Per-step launch parameters.
+struct StepLaunch {
+    const StepArgs *ga = nullptr;  // device copy of the handle's StepArgs
+    int parity = 0;                // read m[parity], write m[parity ^ 1]
+    double *force = nullptr;       // [2][5] FP64 accumulators of a sampled step, or null
+    double *diag_part = nullptr;   // [grid][2] per-CTA mass / energy partials, or null
+    int n_ctas = 0;
+};
+
+// Stencil-buffer index of node (x, y, z) for a special tile slot.
+inline __host__ __device__ int64_t side_index(int slot, int x, int y, int z, int x0, int y0, int nz, int tile_x,
+                                              int tile_y) {
+    return (((int64_t)slot * nz + z) * tile_y + (y - y0)) * tile_x + (x - x0);
+}
+
+// storage: 0 f32, 1 f16, 2 bf16
+cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, cudaStream_t s);
+int step_kernel_smem_bytes(int tile_y);
+int step_kernel_max_ctas_per_sm(int storage, int tile_y);
+// Curved-wall closure + collision for the wall nodes of both walls, plus the force sums.
+cudaError_t launch_wall(const StepLaunch &l, int storage, int n_total, cudaStream_t s);
+// Sum the per-CTA diagnostics partials into out[2] in a fixed order.
+cudaError_t launch_diag_finalize(const double *part, int n, double *out, cudaStream_t s);
+
+struct InitArgs {
+    void *m_a = nullptr, *m_b = nullptr;  // both ping-pong buffers
+    int64_t fs = 0;
+    int nx = 0, ny = 0, nz = 0;
+    int kind = 0;
+    double p[8] = {0};
+    float rho0 = 1.f, u_max = 0.f;
+    StorageScale sc;
+};
+cudaError_t launch_init(const InitArgs &a, int storage, cudaStream_t s);
+
+// Convert between device storage and an FP32 staging buffer (lexicographic or reference
+// tiled layout).  dir = 0: storage -> f32, 1: f32 -> storage (written to dst_a and dst_b).
+cudaError_t launch_convert(const void *src, void *dst_a, void *dst_b, float *f32, int64_t fs, uint32_t field_mask,
+                           int layout, int nx, int ny, int nz, int storage, const StorageScale &sc, int dir,
+                           cudaStream_t s);
+
+}  // namespace mrlbm

@@ -1,0 +1,419 @@
+// Device math of the D3Q27 moment-representation LBM: population reconstruction from
+// the 10 moments, moment evaluation from 27 populations, BGK collision in moment space,
+// and the boundary closures of the planar walls and of the BCFLUID nodes.
+//
+// Reference (paths inside sakthi-lbm/MRLBM_3D_CUDA):
+//   pop_reconstruction   MRLBM_3D/src/core/D3Q27/second_order/reconstruction.cuh:5-60
+//   evaluate_moments     MRLBM_3D/src/core/D3Q27/eval_moments.cuh:5-22
+//   moment_collision     MRLBM_3D/src/solver/mlbm.cu:3-16
+//   boundary_condition   MRLBM_3D/src/cases/cylinder/boundaries.cuh:201-843
+//   update_neumaan_*     MRLBM_3D/src/cases/cylinder/boundaries.cuh:96-199
+//   fluid_boundary_condition  MRLBM_3D/src/cases/cylinder/boundaries.cuh:845-1037
+//   evaluate_incoming_moments_rotated  MRLBM_3D/src/boundary/curvedLBM.cu:5-59
+// The arithmetic is arranged for the GB300 issue budget (shared sub-sums, pair sums);
+// the closures keep the reference's formulas (they are the published solutions of the
+// moment-based boundary method) written once per symmetry class with sign factors.
+#pragma once
+
+#include <cstdint>
+
+#include "lattice_tables.h"
+
+namespace mrlbm {
+
+struct Mom {
+    float rho;  // full density (not the stored deviation)
+    float ux, uy, uz;
+    float mxx, myy, mzz, mxy, mxz, myz;
+};
+
+// f_q = w_q rho [1 + 3 c.u + 4.5 (c_a c_b - delta_ab / 3) m_ab], second-order Hermite.
+__device__ __forceinline__ void reconstruct(const Mom &m, float f[27]) {
+    const float ux = 3.0f * m.ux, uy = 3.0f * m.uy, uz = 3.0f * m.uz;
+    const float xx = 4.5f * m.mxx, yy = 4.5f * m.myy, zz = 4.5f * m.mzz;
+    const float xy = 9.0f * m.mxy, xz = 9.0f * m.mxz, yz = 9.0f * m.myz;
+    const float tr = xx + yy + zz;
+    const float p0 = 1.0f - kCs2 * tr;
+    const float r0 = m.rho * kW0, r1 = m.rho * kW1, r2 = m.rho * kW2, r3 = m.rho * kW3;
+    f[0] = r0 * p0;
+    const float ax = p0 + xx, ay = p0 + yy, az = p0 + zz;
+    f[1] = r1 * (ax + ux);
+    f[2] = r1 * (ax - ux);
+    f[3] = r1 * (ay + uy);
+    f[4] = r1 * (ay - uy);
+    f[5] = r1 * (az + uz);
+    f[6] = r1 * (az - uz);
+    {
+        const float b = ax + yy, sp = ux + uy, sm = ux - uy, cp = b + xy, cm = b - xy;
+        f[7] = r2 * (cp + sp);
+        f[8] = r2 * (cp - sp);
+        f[13] = r2 * (cm + sm);
+        f[14] = r2 * (cm - sm);
+    }
+    {
+        const float b = ax + zz, sp = ux + uz, sm = ux - uz, cp = b + xz, cm = b - xz;
+        f[9] = r2 * (cp + sp);
+        f[10] = r2 * (cp - sp);
+        f[15] = r2 * (cm + sm);
+        f[16] = r2 * (cm - sm);
+    }
+    {
+        const float b = ay + zz, sp = uy + uz, sm = uy - uz, cp = b + yz, cm = b - yz;
+        f[11] = r2 * (cp + sp);
+        f[12] = r2 * (cp - sp);
+        f[17] = r2 * (cm + sm);
+        f[18] = r2 * (cm - sm);
+    }
+    {
+        const float c0 = p0 + tr;
+        const float a = xy + xz, b = xy - xz;
+        const float upp = ux + uy, upm = ux - uy;
+        const float s1 = upp + uz, s2 = upp - uz, s3 = upm + uz, s4 = upm - uz;
+        const float e1 = c0 + (a + yz), e2 = c0 + (b - yz), e3 = c0 - (b + yz), e4 = c0 - (a - yz);
+        f[19] = r3 * (e1 + s1);
+        f[20] = r3 * (e1 - s1);
+        f[21] = r3 * (e2 + s2);
+        f[22] = r3 * (e2 - s2);
+        f[23] = r3 * (e3 + s3);
+        f[24] = r3 * (e3 - s3);
+        f[26] = r3 * (e4 + s4);
+        f[25] = r3 * (e4 - s4);
+    }
+}
+
+// rho = sum f, u = sum c f / rho, m_ab = sum c_a c_b f / rho - cs2 delta_ab, via the 13
+// opposite-pair sums e and differences d.
+__device__ __forceinline__ void evaluate(const float f[27], Mom &m) {
+    const float e1 = f[1] + f[2], d1 = f[1] - f[2];
+    const float e3 = f[3] + f[4], d3 = f[3] - f[4];
+    const float e5 = f[5] + f[6], d5 = f[5] - f[6];
+    const float e7 = f[7] + f[8], d7 = f[7] - f[8];
+    const float e9 = f[9] + f[10], d9 = f[9] - f[10];
+    const float e11 = f[11] + f[12], d11 = f[11] - f[12];
+    const float e13 = f[13] + f[14], d13 = f[13] - f[14];
+    const float e15 = f[15] + f[16], d15 = f[15] - f[16];
+    const float e17 = f[17] + f[18], d17 = f[17] - f[18];
+    const float e19 = f[19] + f[20], d19 = f[19] - f[20];
+    const float e21 = f[21] + f[22], d21 = f[21] - f[22];
+    const float e23 = f[23] + f[24], d23 = f[23] - f[24];
+    const float e25 = f[25] + f[26], d25 = f[25] - f[26];
+    const float ec = (e19 + e21) + (e23 + e25);
+    const float sxx = (e1 + e7) + (e9 + e13) + e15 + ec;
+    const float syy = (e3 + e7) + (e11 + e13) + e17 + ec;
+    const float szz = (e5 + e9) + (e11 + e15) + e17 + ec;
+    const float rho = f[0] + ((e1 + e3) + e5) + ((e7 + e9) + (e11 + e13)) + ((e15 + e17) + ec);
+    const float jx = (d1 + d7) + (d9 + d13) + (d15 + d19) + (d21 + d23) - d25;
+    const float jy = (d3 + d7) + (d11 - d13) + (d17 + d19) + (d21 - d23) + d25;
+    const float jz = (d5 + d9) + (d11 - d15) - (d17 - d19) + (d23 - d21) + d25;
+    const float sxy = (e7 - e13) + ((e19 + e21) - (e23 + e25));
+    const float sxz = (e9 - e15) + ((e19 - e21) + (e23 - e25));
+    const float syz = (e11 - e17) + ((e19 - e21) - (e23 - e25));
+    const float inv = 1.0f / rho;
+    m.rho = rho;
+    m.ux = jx * inv;
+    m.uy = jy * inv;
+    m.uz = jz * inv;
+    m.mxx = sxx * inv - kCs2;
+    m.myy = syy * inv - kCs2;
+    m.mzz = szz * inv - kCs2;
+    m.mxy = sxy * inv;
+    m.mxz = sxz * inv;
+    m.myz = syz * inv;
+}
+
+// m_ab <- (1 - omega) m_ab + omega u_a u_b; rho and u are collision invariants.
+__device__ __forceinline__ void collide(Mom &m, float omega) {
+    const float om1 = 1.0f - omega;
+    m.mxx = om1 * m.mxx + omega * m.ux * m.ux;
+    m.myy = om1 * m.myy + omega * m.uy * m.uy;
+    m.mzz = om1 * m.mzz + omega * m.uz * m.uz;
+    m.mxy = om1 * m.mxy + omega * m.ux * m.uy;
+    m.mxz = om1 * m.mxz + omega * m.ux * m.uz;
+    m.myz = om1 * m.myz + omega * m.uy * m.uz;
+}
+
+// ---------------------------------------------------------------------------------------
+// Boundary closures (rare nodes; kept out of the bulk path with __noinline__ callers).
+
+// Walls of a planar boundary class, as bits W=1 E=2 S=4 N=8 B=16 F=32.
+__device__ __forceinline__ uint32_t class_walls(uint32_t c) {
+    // classes 8..33 of the reference enum, in order
+    constexpr uint8_t kWalls[34] = {0, 0, 0, 0, 0, 0, 0, 0,
+                                    8, 4, 2, 1, 32, 16,            // N S E W F B
+                                    10, 9, 40, 24, 6, 5, 36, 20,   // NE NW NF NB SE SW SF SB
+                                    34, 18, 33, 17,                // EF EB WF WB
+                                    41, 25, 37, 21, 42, 26, 38, 22};  // NWF NWB SWF SWB NEF NEB SEF SEB
+    return c < 34 ? kWalls[c] : 0u;
+}
+
+// Directions whose population is known after streaming at a node on walls `w`: a wall
+// removes the populations that would come from outside the grid.
+__device__ __forceinline__ bool known_dir(uint32_t w, int q) {
+    const int cx = cxq(q), cy = cyq(q), cz = czq(q);
+    return !(((w & 1u) && cx == 1) || ((w & 2u) && cx == -1) || ((w & 4u) && cy == 1) ||
+             ((w & 8u) && cy == -1) || ((w & 16u) && cz == 1) || ((w & 32u) && cz == -1));
+}
+
+struct Partial {
+    float rho;                 // sum over known populations
+    float sxx, syy, szz;       // sum c_a^2 f (known)
+    float sxy, sxz, syz;       // sum c_a c_b f (known)
+};
+
+__device__ __forceinline__ Partial known_sums(uint32_t w, const float f[27]) {
+    Partial p{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 27; ++q) {
+        if (!known_dir(w, q)) continue;
+        const float v = f[q];
+        p.rho += v;
+        if (cxq(q)) p.sxx += v;
+        if (cyq(q)) p.syy += v;
+        if (czq(q)) p.szz += v;
+        if (cxq(q) * cyq(q) > 0) p.sxy += v;
+        if (cxq(q) * cyq(q) < 0) p.sxy -= v;
+        if (cxq(q) * czq(q) > 0) p.sxz += v;
+        if (cxq(q) * czq(q) < 0) p.sxz -= v;
+        if (cyq(q) * czq(q) > 0) p.syz += v;
+        if (cyq(q) * czq(q) < 0) p.syz -= v;
+    }
+    return p;
+}
+
+struct PlanarCtx {
+    float omega;
+    float u_max;
+    float rho0;
+    int convective;
+    // pre-stream moments of the node and of its x-1 neighbour (outlet extrapolation)
+    Mom self_prev;
+    Mom west_prev;
+};
+
+// Zero-gradient outlet from the x-1 neighbour, optionally blended with the node itself
+// by Uc = |u_x| of the neighbour (update_neumaan_density_velocity, boundaries.cuh:163-199).
+__device__ __forceinline__ void outlet_rho_u(const PlanarCtx &c, Mom &o) {
+    const Mom &i = c.west_prev;
+    if (c.convective) {
+        const Mom &b = c.self_prev;
+        const float uc = sqrtf(i.ux * i.ux);
+        const double w = 1.0 - (double)uc;
+        o.rho = (float)(w * (double)b.rho + (double)(uc * i.rho));
+        o.ux = (float)(w * (double)b.ux + (double)(uc * i.ux));
+        o.uy = (float)(w * (double)b.uy + (double)(uc * i.uy));
+        o.uz = (float)(w * (double)b.uz + (double)(uc * i.uz));
+    } else {
+        o.rho = i.rho;
+        o.ux = i.ux;
+        o.uy = i.uy;
+        o.uz = i.uz;
+    }
+}
+
+// Planar face / edge / corner closures.  Returns false for classes without one (the node
+// keeps its pre-stream moments, like the reference's switch default).
+__device__ __forceinline__ bool planar_closure(uint32_t cls, const float f[27], const PlanarCtx &c, Mom &o) {
+    const uint32_t w = class_walls(cls);
+    if (!w) return false;
+    const int nw = __popc(w);
+    const bool east = (w & 2u) != 0, west = (w & 1u) != 0;
+    const float om = c.omega;
+    if (nw == 3) {
+        // corners: west corners are no-slip with rho = 216/125 rho_I, east corners extrapolate
+        if (east) {
+            outlet_rho_u(c, o);
+        } else {
+            const Partial p = known_sums(w, f);
+            o.rho = 216.0f * p.rho / 125.0f;
+            o.ux = o.uy = o.uz = 0.0f;
+        }
+        o.mxx = o.myy = o.mzz = o.mxy = o.mxz = o.myz = 0.0f;
+        return true;
+    }
+    const Partial p = known_sums(w, f);
+    const float ri = p.rho, inv = 1.0f / ri;
+    if (nw == 1) {
+        if (west) {  // velocity inlet u = (U, 0, 0); rho from the known populations and the
+                     // pre-stream u_x (boundaries.cuh:206-229)
+            const float mxy_i = p.sxy * inv, mxz_i = p.sxz * inv;
+            const float u0 = c.self_prev.ux;
+            o.rho = -6.0f * ri / (-5.0f + 3.0f * u0 + 3.0f * u0 * u0);
+            o.ux = c.u_max;
+            o.uy = o.uz = 0.0f;
+            o.mxx = o.ux * o.ux;
+            o.myy = o.mzz = 0.0f;
+            o.mxy = 2.0f * mxy_i * ri / o.rho;
+            o.mxz = 2.0f * mxz_i * ri / o.rho;
+            o.myz = 0.0f;
+        } else if (east) {  // outlet (boundaries.cuh:230-271)
+            const float myy_i = p.syy * inv - kCs2, mzz_i = p.szz * inv - kCs2;
+            const float mxy_i = p.sxy * inv, mxz_i = p.sxz * inv, myz_i = p.syz * inv;
+            outlet_rho_u(c, o);
+            const float r = o.rho;
+            o.mxx = o.ux * o.ux;
+            o.myy = (6.0f * myy_i * ri - 6.0f * mzz_i * ri + 5.0f * o.uy * o.uy * r + 5.0f * o.uz * o.uz * r) / (10.0f * r);
+            o.mzz = (-6.0f * myy_i * ri + 6.0f * mzz_i * ri + 5.0f * o.uy * o.uy * r + 5.0f * o.uz * o.uz * r) / (10.0f * r);
+            o.mxy = (6.0f * mxy_i * ri - o.uy * r) / (3.0f * r);
+            o.mxz = (6.0f * mxz_i * ri - o.uz * r) / (3.0f * r);
+            o.myz = 6.0f * myz_i * ri / (5.0f * r);
+        } else {  // no-slip face normal to y (N, S) or z (F, B)
+            o.rho = 6.0f * ri / 5.0f;
+            o.ux = o.uy = o.uz = 0.0f;
+            o.mxx = o.myy = o.mzz = 0.0f;
+            const bool ynormal = (w & 12u) != 0;
+            o.mxy = ynormal ? 2.0f * (p.sxy * inv) * ri / o.rho : 0.0f;
+            o.mxz = ynormal ? 0.0f : 2.0f * (p.sxz * inv) * ri / o.rho;
+            o.myz = 2.0f * (p.syz * inv) * ri / o.rho;
+        }
+        return true;
+    }
+    // edges: the two normal axes a < b carry m_ab; sigma = -s_a s_b, s = +1 on the max face
+    const bool xa = (w & 3u) != 0, ya = (w & 12u) != 0;
+    const float sa = (w & 2u) ? 1.f : ((w & 1u) ? -1.f : ((w & 8u) ? 1.f : -1.f));
+    const float sb = (w & 32u) ? 1.f : ((w & 16u) ? -1.f : ((w & 8u) ? 1.f : -1.f));
+    const float sigma = -sa * sb;
+    float m_i, t_i;  // normal-pair moment and, for x-edges, the other normal with the tangent
+    if (xa && ya) { m_i = p.sxy * inv; t_i = p.syz * inv; }
+    else if (xa) { m_i = p.sxz * inv; t_i = p.syz * inv; }
+    else { m_i = p.syz * inv; t_i = 0.f; }
+    if (east) {
+        outlet_rho_u(c, o);
+    } else {
+        o.rho = sigma > 0.f ? 36.0f * ri * (1.0f + m_i - m_i * om) / (24.0f + om)
+                            : 36.0f * ri * (1.0f - m_i + m_i * om) / (24.0f + om);
+        o.ux = o.uy = o.uz = 0.0f;
+    }
+    const float r = o.rho;
+    const float mab = sigma > 0.f ? (36.0f * m_i * ri + r) / (9.0f * r) : (36.0f * m_i * ri - r) / (9.0f * r);
+    o.mxx = o.myy = o.mzz = 0.0f;
+    if (xa && ya) { o.mxy = mab; o.mxz = 0.0f; o.myz = 12.0f * t_i * ri / (5.0f * r); }
+    else if (xa) { o.mxy = 0.0f; o.mxz = mab; o.myz = 12.0f * t_i * ri / (5.0f * r); }
+    else { o.mxy = 0.0f; o.mxz = 0.0f; o.myz = mab; }
+    return true;
+}
+
+// Incoming partial moments over `mask`, with the lattice Hermite tensors (the reference's
+// d_H** tables hold c_a c_b - cs2 delta_ab in float).
+struct Incoming {
+    float rho, ux, uy, uz, mxx, myy, mzz, mxy, mxz, myz;
+};
+__device__ __forceinline__ Incoming incoming_moments(uint32_t mask, const float f[27]) {
+    Incoming s{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 27; ++q) {
+        if (!(mask & (1u << q))) continue;
+        const float v = f[q];
+        const float cx = (float)cxq(q), cy = (float)cyq(q), cz = (float)czq(q);
+        s.rho += v;
+        s.ux += v * cx;
+        s.uy += v * cy;
+        s.uz += v * cz;
+        s.mxx += v * (cx * cx - kCs2);
+        s.myy += v * (cy * cy - kCs2);
+        s.mzz += v * (cz * cz - kCs2);
+        s.mxy += v * (cx * cy);
+        s.mxz += v * (cx * cz);
+        s.myz += v * (cy * cz);
+    }
+    const float inv = 1.0f / s.rho;
+    s.ux *= inv; s.uy *= inv; s.uz *= inv;
+    s.mxx *= inv; s.myy *= inv; s.mzz *= inv;
+    s.mxy *= inv; s.mxz *= inv; s.myz *= inv;
+    return s;
+}
+
+// BCFLUID closure for the four diagonal-quadrant tags 17, 34, 68, 136 (solid octant pair
+// below/above in z at (-x,-y), (+x,-y), (-x,+y), (+x,+y)).  (sx, sy) point from the solid
+// quadrant into the fluid.  Returns false for other tags (moments stay pre-stream).
+__device__ __forceinline__ bool bcfluid_closure(uint32_t tag, uint32_t mask, const float f[27], int strong,
+                                                float omega, Mom &o) {
+    float sx, sy;
+    if (tag == 17u) { sx = 1.f; sy = 1.f; }
+    else if (tag == 34u) { sx = -1.f; sy = 1.f; }
+    else if (tag == 68u) { sx = 1.f; sy = -1.f; }
+    else if (tag == 136u) { sx = -1.f; sy = -1.f; }
+    else return false;
+    const Incoming I = incoming_moments(mask, f);
+    const float rI = I.rho, mxx = I.mxx, myy = I.myy, mzz = I.mzz, mxy = I.mxy, mxz = I.mxz, myz = I.myz;
+    const float ux = I.ux, uy = I.uy, uz = I.uz;
+    const float sxy = sx * sy;
+    const float us = sx * ux + sy * uy;
+    const float poly = 45.0f * (mxx * mxx) + 405.0f * (mxy * mxy) + 45.0f * (myy * myy) + (345.0f * sx) * myy * ux +
+                       589.0f * (ux * ux) + (345.0f * sy) * myy * uy + (1467.0f * sxy) * ux * uy + 589.0f * (uy * uy) +
+                       (45.0f * sxy) * mxy * (6.0f * myy + 23.0f * us) +
+                       15.0f * mxx * ((18.0f * sxy) * mxy + 6.0f * myy + 23.0f * us);
+    float a, b, cc;
+    if (strong) {  // MassBC::Strong quadratic (boundaries.cuh:890-897 and its mirror images)
+        a = -9996.0f - 206.0f * omega;
+        b = -6.0f * rI *
+            (12.0f * mxx * (-17.0f + 20.0f * omega) -
+             17.0f * (102.0f + (36.0f * sxy) * mxy + 12.0f * myy - (5.0f * sx) * ux - (5.0f * sy) * uy) +
+             omega * ((720.0f * sxy) * mxy + 240.0f * myy + 53.0f * us));
+        cc = 3.0f * omega * (rI * rI) * poly;
+    } else {  // MassBC::Equilibrium quadratic
+        a = -9998.0f;
+        b = 6.0f * rI * (1734.0f + 66.0f * mxx + (198.0f * sxy) * mxy + 66.0f * myy + (253.0f * sx) * ux + (253.0f * sy) * uy);
+        cc = 3.0f * (rI * rI) * poly;
+    }
+    const float disc = fmaxf(b * b - 4.0f * a * cc, 0.0f);
+    const float sq = sqrtf(disc);
+    const float r1 = (-b + sq) / (2.0f * a), r2 = (-b - sq) / (2.0f * a);
+    const float r = (r1 > 0.0f && fabsf(r1 - rI) < fabsf(r2 - rI)) ? r1 : r2;
+    o.rho = r;
+    o.ux = sx * (3.0f * mxx * rI + (9.0f * sxy) * mxy * rI + 3.0f * myy * rI + (20.0f * sx) * rI * ux + (3.0f * sy) * rI * uy + r) / (17.0f * r);
+    o.uy = sy * (3.0f * mxx * rI + (9.0f * sxy) * mxy * rI + 3.0f * myy * rI + (3.0f * sx) * rI * ux + (20.0f * sy) * rI * uy + r) / (17.0f * r);
+    o.uz = (3.0f * rI * (sx * mxz + sy * myz + 10.0f * uz)) / (29.0f * r);
+    o.mxx = (57.0f * mxx * rI + (18.0f * sxy) * mxy * rI + 6.0f * myy * rI + (6.0f * sx) * rI * ux + (6.0f * sy) * rI * uy + 2.0f * r) / (51.0f * r);
+    o.myy = (6.0f * mxx * rI + (18.0f * sxy) * mxy * rI + 57.0f * myy * rI + (6.0f * sx) * rI * ux + (6.0f * sy) * rI * uy + 2.0f * r) / (51.0f * r);
+    o.mzz = (36.0f * mzz * rI) / (35.0f * r);
+    o.mxy = sxy * (3.0f * mxx * rI + (26.0f * sxy) * mxy * rI + 3.0f * myy * rI + (3.0f * sx) * rI * ux + (3.0f * sy) * rI * uy + r) / (17.0f * r);
+    o.mxz = (rI * (32.0f * mxz + (3.0f * sxy) * myz + sx * uz)) / (29.0f * r);
+    o.myz = (rI * ((3.0f * sxy) * mxz + 32.0f * myz + sy * uz)) / (29.0f * r);
+    return true;
+}
+
+// Incoming rho and second moments at a curved-wall node in the frame rotated to its
+// normal (cos = nx, sin = ny); u is left to the wall kernel.
+__device__ __forceinline__ void incoming_rotated(float nx, float ny, uint32_t mask, const float f[27], Mom &o) {
+    float r = 0.f, sxx = 0.f, syy = 0.f, szz = 0.f, sxy = 0.f, sxz = 0.f, syz = 0.f;
+#pragma unroll
+    for (int q = 0; q < 27; ++q) {
+        if (!(mask & (1u << q))) continue;
+        const float cx = (float)cxq(q), cy = (float)cyq(q), cz = (float)czq(q);
+        const float cxp = cx * nx + cy * ny;
+        const float cyp = -cx * ny + cy * nx;
+        const float czp = cz;
+        const float v = f[q];
+        r += v;
+        sxx += v * (cxp * cxp - kCs2);
+        syy += v * (cyp * cyp - kCs2);
+        szz += v * (czp * czp - kCs2);
+        sxy += v * (cxp * cyp);
+        sxz += v * (cxp * czp);
+        syz += v * (cyp * czp);
+    }
+    const float inv = 1.0f / r;
+    o.rho = r;
+    o.mxx = sxx * inv;
+    o.myy = syy * inv;
+    o.mzz = szz * inv;
+    o.mxy = sxy * inv;
+    o.mxz = sxz * inv;
+    o.myz = syz * inv;
+}
+
+// Momentum and mass carried by the populations of `mask` (compute_forces_mass, forces.cu:3-23).
+__device__ __forceinline__ void masked_momentum(uint32_t mask, const float f[27], float &fx, float &fy, float &fz,
+                                                float &fm) {
+    fx = fy = fz = fm = 0.f;
+#pragma unroll
+    for (int q = 0; q < 27; ++q) {
+        if (!(mask & (1u << q))) continue;
+        fx += f[q] * (float)cxq(q);
+        fy += f[q] * (float)cyq(q);
+        fz += f[q] * (float)czq(q);
+        fm += f[q];
+    }
+}
+
+}  // namespace mrlbm

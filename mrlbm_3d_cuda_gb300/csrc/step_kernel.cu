@@ -1,0 +1,427 @@
+// Fused MR-LBM time step: stream + moment evaluation / boundary closure + collision in one
+// pass over HBM (one moment read, one moment write per node).
+//
+// Replaces the reference's two full-grid kernels and their population halo
+// (paths inside sakthi-lbm/MRLBM_3D_CUDA):
+//   streaming_and_evaluate_Mom  MRLBM_3D/src/solver/mlbm.cu:83-164
+//   collision_halo_update       MRLBM_3D/src/solver/mlbm.cu:186-242
+//   pop_load_from_halo / pop_save_to_halo / save_pop / streaming
+//                               MRLBM_3D/src/core/D3Q27/halo_interface.cuh:5-201, core/streaming.cuh:6-35
+// The reference streams populations rebuilt from the stored (post-collision) moments:
+// f_q(x) = R(M(x - c_q))_q on a grid that wraps in every axis, then evaluates moments or a
+// boundary closure, then collides.  Here each CTA owns a 32 x TY column of nodes and marches
+// along z.  For every plane it rebuilds the populations of the column plus a one-node rim
+// (neighbour moments read through L2) into shared-memory ring buffers split by c_z, so a
+// node's 27 pulled populations come from planes z-1, z, z+1 without any population array in
+// HBM.  Post-collision moments go to the second ping-pong buffer.
+#include <cstdio>
+
+#include "mrlbm_internal.h"
+#include "storage.cuh"
+
+namespace mrlbm {
+namespace {
+
+// Populations exchanged through shared memory, split by c_z (the three c = (0,0,c_z)
+// populations stay in registers of the column's owner thread).
+// Eight 5-bit direction indices per class packed in one constant:
+//   up   (c_z = +1, pulled from plane z-1): 9, 11, 16, 18, 19, 22, 23, 25
+//   flat (c_z =  0, pulled from plane z):   1, 2, 3, 4, 7, 8, 13, 14
+//   down (c_z = -1, pulled from plane z+1): 10, 12, 15, 17, 20, 21, 24, 26
+constexpr unsigned long long pack5(int a, int b, int c, int d, int e, int f, int g, int h) {
+    return (unsigned long long)a | (unsigned long long)b << 5 | (unsigned long long)c << 10 |
+           (unsigned long long)d << 15 | (unsigned long long)e << 20 | (unsigned long long)f << 25 |
+           (unsigned long long)g << 30 | (unsigned long long)h << 35;
+}
+constexpr unsigned long long kUpBits = pack5(9, 11, 16, 18, 19, 22, 23, 25);
+constexpr unsigned long long kFlBits = pack5(1, 2, 3, 4, 7, 8, 13, 14);
+constexpr unsigned long long kDnBits = pack5(10, 12, 15, 17, 20, 21, 24, 26);
+__host__ __device__ constexpr int hUp(int j) { return (int)((kUpBits >> (5 * j)) & 31ull); }
+__host__ __device__ constexpr int hFl(int j) { return (int)((kFlBits >> (5 * j)) & 31ull); }
+__host__ __device__ constexpr int hDn(int j) { return (int)((kDnBits >> (5 * j)) & 31ull); }
+
+template <int TY>
+struct Geo {
+    static constexpr int NTH = TILE_X * TY;
+    static constexpr int W = TILE_X + 2;        // shared-memory row pitch (column + rim)
+    static constexpr int NCOL = W * (TY + 2);   // columns incl. rim
+    static constexpr int NR = 2 * TILE_X + 2 * TY + 4;
+    static constexpr int PLANE = 8 * NCOL;      // floats of one 8-population plane buffer
+    static constexpr int SMEM = 6 * PLANE * 4;  // up x3, flat x2, down x1
+};
+
+constexpr bool need_dir(int q, int rcx, int rcy) {
+    return (rcx == 0 || cxq(q) == rcx) && (rcy == 0 || cyq(q) == rcy);
+}
+
+// Rebuild the populations of one rim column and store the ones the tile pulls from it
+// (rcx, rcy: the c_x / c_y a population must have to enter the tile from this rim side).
+template <int RCX, int RCY, int TY>
+__device__ __forceinline__ void rim_store(const Mom &m, float *up, float *fl, float *dn, int col) {
+    constexpr int NC = Geo<TY>::NCOL;
+    float f[27];
+    reconstruct(m, f);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (need_dir(hUp(j), RCX, RCY)) up[j * NC + col] = f[hUp(j)];
+        if (need_dir(hFl(j), RCX, RCY)) fl[j * NC + col] = f[hFl(j)];
+        if (need_dir(hDn(j), RCX, RCY)) dn[j * NC + col] = f[hDn(j)];
+    }
+}
+
+// Non-bulk node: boundary closure, stencil snapshot, BCFLUID force.  Works on a private
+// copy of the pulled populations so the bulk path keeps its registers.  Returns 0 when the
+// node is not stored here, 1 to store the collided moments `m`, 2 to store them and count
+// the node in the fluid diagnostics.
+template <typename S, int TY>
+__device__ __noinline__ int special_node(const StepArgs *__restrict__ ga, int parity, bool force, uint32_t w,
+                                         float *fl, int x, int y, int z, int64_t node, int slot, int x0, int y0,
+                                         Mom &m) {
+    if (w & NW_FROZEN) return 0;  // block the reference never updates
+    const StepArgs &a = *ga;
+    const uint32_t cls = w & NW_CLASS_MASK;
+    const S *__restrict__ src = (const S *)a.m[parity];
+    bool wall_node = false;
+    bool fluid = true;
+    if (cls == C_BULK) {
+        evaluate(fl, m);
+    } else {
+        const Mom prev = load_mom<S>(src, a.fs, node, a.rho0, a.sc);
+        m = prev;  // nodes without a closure keep their pre-stream moments
+        if (cls == C_SOLID) {
+            fluid = false;
+        } else if (cls == C_INNER || cls == C_OUTER) {
+            const int wi = cls == C_INNER ? 0 : 1;
+            const uint32_t bi = w >> NW_PAYLOAD_SHIFT;
+            incoming_rotated(a.wall[wi].nx[bi], a.wall[wi].ny[bi], a.wall[wi].in_mask[bi], fl, m);
+            wall_node = true;
+            fluid = false;
+        } else if (cls == C_BCFLUID_INNER || cls == C_BCFLUID_OUTER) {
+            const uint32_t tag = (w >> NW_PAYLOAD_SHIFT) & 0xFFu;
+            Mom o = prev;
+            if (bcfluid_closure(tag, a.tag_in[tag], fl, a.bcf_strong, a.omega, o)) m = o;
+        } else {
+            PlanarCtx c;
+            c.omega = a.omega;
+            c.u_max = a.u_max;
+            c.rho0 = a.rho0;
+            c.convective = a.convective;
+            c.self_prev = prev;
+            if (class_walls(cls) & 2u) c.west_prev = load_mom<S>(src, a.fs, node - 1, a.rho0, a.sc);
+            else c.west_prev = prev;
+            Mom o = prev;
+            if (planar_closure(cls, fl, c, o)) m = o;
+        }
+    }
+    if ((w & NW_STENCIL) && slot >= 0) {
+        float *e = a.side + side_index(slot, x, y, z, x0, y0, a.nz, TILE_X, TY) * 16;
+        e[0] = m.rho - a.rho0;
+        e[1] = m.ux; e[2] = m.uy; e[3] = m.uz;
+        e[4] = m.mxx; e[5] = m.myy; e[6] = m.mzz;
+        e[7] = m.mxy; e[8] = m.mxz; e[9] = m.myz;
+    }
+    if (wall_node) return 0;  // the wall kernel finishes this node
+    const bool bcf = force && slot >= 0 && (cls == C_BCFLUID_INNER || cls == C_BCFLUID_OUTER);
+    float fin[4] = {0.f, 0.f, 0.f, 0.f};
+    const uint32_t tag = (w >> NW_PAYLOAD_SHIFT) & 0xFFu;
+    if (bcf) {
+        reconstruct(m, fl);
+        masked_momentum(a.tag_in[tag], fl, fin[0], fin[1], fin[2], fin[3]);
+    }
+    collide(m, a.omega);
+    if (bcf) {
+        float fo[4];
+        reconstruct(m, fl);
+        masked_momentum(a.tag_out[tag], fl, fo[0], fo[1], fo[2], fo[3]);
+        float *e = a.side + side_index(slot, x, y, z, x0, y0, a.nz, TILE_X, TY) * 16;
+        e[10] = fin[0] - fo[0];
+        e[11] = fin[1] - fo[1];
+        e[12] = fin[2] - fo[2];
+        e[13] = fin[3] - fo[3];
+    }
+    return fluid ? 2 : 1;
+}
+
+template <typename S, int TY>
+__global__ void __launch_bounds__(TILE_X *TY, (TY == 4 ? 5 : (TY == 8 ? 3 : 1)))
+    step_kernel(const StepArgs *__restrict__ ga, const int parity, double *__restrict__ force,
+                double *__restrict__ diag_part) {
+    using G = Geo<TY>;
+    extern __shared__ float smem[];
+    __shared__ double red[2][TY];
+    const S *__restrict__ src = (const S *)ga->m[parity];
+    S *__restrict__ dst = (S *)ga->m[parity ^ 1];
+    const int64_t fs = ga->fs;
+    const int nx = ga->nx, ny = ga->ny, nz = ga->nz, lz = ga->lz, tiles_x = ga->tiles_x, n_items = ga->n_items;
+    const int32_t *__restrict__ items = ga->items;
+    const int32_t *__restrict__ tile_slot = ga->tile_slot;
+    const uint32_t *__restrict__ word = ga->word;
+    const float omega = ga->omega, rho0 = ga->rho0;
+    const StorageScale sc = ga->sc;
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int64_t plane = (int64_t)nx * ny;
+    double dmD = 0.0, deD = 0.0;
+
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const int item = items[it];
+        const int tile = item & 0xFFFFF, seg = item >> 20;
+        const int tix = tile % tiles_x, tiy = tile / tiles_x;
+        const int x0 = tix * TILE_X, y0 = tiy * TY;
+        const int w = min(TILE_X, nx - x0), h = min(TY, ny - y0);
+        const int zs = seg * lz, ze = min(zs + lz, nz);
+        const int slot = tile_slot ? tile_slot[tile] : -1;
+        const bool own = tx < w && ty < h;
+        const int x = x0 + tx, y = y0 + ty;
+        const int col = (ty + 1) * G::W + (tx + 1);
+        const int64_t xy = own ? (int64_t)x + (int64_t)nx * y : 0;
+
+        // rim column of this thread (if any)
+        int rside = -1, rcol = 0;
+        int64_t rxy = 0;
+        if (tid < G::NR) {
+            int rx, ry, sd;
+            const int r = tid;
+            if (r < TILE_X) { rx = r; ry = -1; sd = 0; }
+            else if (r < 2 * TILE_X) { rx = r - TILE_X; ry = h; sd = 1; }
+            else if (r < 2 * TILE_X + TY) { rx = -1; ry = r - 2 * TILE_X; sd = 2; }
+            else if (r < 2 * TILE_X + 2 * TY) { rx = w; ry = r - 2 * TILE_X - TY; sd = 3; }
+            else {
+                const int k = r - 2 * TILE_X - 2 * TY;
+                rx = (k & 1) ? w : -1;
+                ry = (k & 2) ? h : -1;
+                sd = 4 + k;
+            }
+            const bool valid = (sd == 0 || sd == 1) ? rx < w : ((sd == 2 || sd == 3) ? ry < h : true);
+            if (valid) {
+                rside = sd;
+                rcol = (ry + 1) * G::W + (rx + 1);
+                const int gx = (x0 + rx + nx) % nx, gy = (y0 + ry + ny) % ny;
+                rxy = (int64_t)gx + (int64_t)nx * gy;
+            }
+        }
+
+        float pre[10];
+        float c0 = 0.f, c5 = 0.f, c6 = 0.f;  // own-column rest / up / down populations of the newest plane
+        float p0 = 0.f, p5 = 0.f, pp5 = 0.f; // history: f0(z), f5(z), f5(z-1)
+        float dm = 0.f, de = 0.f;
+
+        auto plane_of = [&](int p) -> int64_t { return (int64_t)((p + nz) % nz) * plane; };
+        if (own) load_raw<S>(src, fs, xy + plane_of(zs - 1), pre);
+
+        // arrive(p): rebuild the populations of plane p into ring slot k
+        auto arrive = [&](int p, int k) {
+            float *up = smem + (k % 3) * G::PLANE;
+            float *fl = smem + (3 + (k & 1)) * G::PLANE;
+            float *dn = smem + 5 * G::PLANE;
+            float rv[10];
+            if (rside >= 0) load_raw<S>(src, fs, rxy + plane_of(p), rv);
+            if (own) {
+                const Mom m = decode<S>(pre, rho0, sc);
+                if (p + 1 <= ze) load_raw<S>(src, fs, xy + plane_of(p + 1), pre);
+                float f[27];
+                reconstruct(m, f);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    up[j * G::NCOL + col] = f[hUp(j)];
+                    fl[j * G::NCOL + col] = f[hFl(j)];
+                    dn[j * G::NCOL + col] = f[hDn(j)];
+                }
+                c0 = f[0];
+                c5 = f[5];
+                c6 = f[6];
+            }
+            if (rside >= 0) {
+                const Mom m = decode<S>(rv, rho0, sc);
+                switch (rside) {
+                    case 0: rim_store<0, 1, TY>(m, up, fl, dn, rcol); break;
+                    case 1: rim_store<0, -1, TY>(m, up, fl, dn, rcol); break;
+                    case 2: rim_store<1, 0, TY>(m, up, fl, dn, rcol); break;
+                    case 3: rim_store<-1, 0, TY>(m, up, fl, dn, rcol); break;
+                    case 4: rim_store<1, 1, TY>(m, up, fl, dn, rcol); break;
+                    case 5: rim_store<-1, 1, TY>(m, up, fl, dn, rcol); break;
+                    case 6: rim_store<1, -1, TY>(m, up, fl, dn, rcol); break;
+                    default: rim_store<-1, -1, TY>(m, up, fl, dn, rcol); break;
+                }
+            }
+        };
+
+        arrive(zs - 1, 0);
+        p5 = c5;
+        arrive(zs, 1);
+        pp5 = p5;
+        p5 = c5;
+        p0 = c0;
+        for (int z = zs; z < ze; ++z) {
+            const int k = z - zs + 1;
+            arrive(z + 1, k + 1);
+            __syncthreads();
+            if (own) {
+                const float *up = smem + ((k - 1) % 3) * G::PLANE;
+                const float *fl = smem + (3 + (k & 1)) * G::PLANE;
+                const float *dn = smem + 5 * G::PLANE;
+                float f[27];
+                f[0] = p0;
+                f[5] = pp5;
+                f[6] = c6;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    f[hUp(j)] = up[j * G::NCOL + col - cyq(hUp(j)) * G::W - cxq(hUp(j))];
+                    f[hFl(j)] = fl[j * G::NCOL + col - cyq(hFl(j)) * G::W - cxq(hFl(j))];
+                    f[hDn(j)] = dn[j * G::NCOL + col - cyq(hDn(j)) * G::W - cxq(hDn(j))];
+                }
+                const int64_t node = xy + (int64_t)z * plane;
+                const uint32_t wd = slot >= 0 ? word[node] : 0u;
+                if (wd == 0u) {
+                    Mom m;
+                    evaluate(f, m);
+                    dm += m.rho - rho0;
+                    de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
+                    collide(m, omega);
+                    store_mom<S>(dst, fs, node, m, rho0, sc);
+                } else {
+                    float fw[27];
+#pragma unroll
+                    for (int q = 0; q < 27; ++q) fw[q] = f[q];
+                    Mom ms;
+                    const int code =
+                        special_node<S, TY>(ga, parity, force != nullptr, wd, fw, x, y, z, node, slot, x0, y0, ms);
+                    if (code) store_mom<S>(dst, fs, node, ms, rho0, sc);
+                    if (code == 2) {
+                        dm += ms.rho - rho0;
+                        de += 0.5f * (ms.ux * ms.ux + ms.uy * ms.uy + ms.uz * ms.uz);
+                    }
+                }
+            }
+            __syncthreads();
+            pp5 = p5;
+            p5 = c5;
+            p0 = c0;
+        }
+        dmD += (double)dm;
+        deD += (double)de;
+    }
+
+    if (diag_part) {
+        // deterministic block reduction of the FP64 partials -> diag_part[blockIdx.x]
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            dmD += __shfl_down_sync(0xffffffffu, dmD, o);
+            deD += __shfl_down_sync(0xffffffffu, deD, o);
+        }
+        if (tx == 0) {
+            red[0][ty] = dmD;
+            red[1][ty] = deD;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double s0 = 0.0, s1 = 0.0;
+            for (int i = 0; i < TY; ++i) {
+                s0 += red[0][i];
+                s1 += red[1][i];
+            }
+            diag_part[2 * blockIdx.x + 0] = s0;
+            diag_part[2 * blockIdx.x + 1] = s1;
+        }
+    }
+}
+
+__global__ void diag_finalize_kernel(const double *__restrict__ part, int n, double *__restrict__ out) {
+    __shared__ double s[2][256];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        a += part[2 * i];
+        b += part[2 * i + 1];
+    }
+    s[0][threadIdx.x] = a;
+    s[1][threadIdx.x] = b;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            s[0][threadIdx.x] += s[0][threadIdx.x + o];
+            s[1][threadIdx.x] += s[1][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = s[0][0];
+        out[1] = s[1][0];
+    }
+}
+
+template <typename S, int TY>
+cudaError_t launch_t(const StepLaunch &l, cudaStream_t s) {
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(step_kernel<S, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             Geo<TY>::SMEM);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    step_kernel<S, TY><<<l.n_ctas, Geo<TY>::NTH, Geo<TY>::SMEM, s>>>(l.ga, l.parity, l.force, l.diag_part);
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_s(const StepLaunch &l, int tile_y, cudaStream_t s) {
+    switch (tile_y) {
+        case 4: return launch_t<S, 4>(l, s);
+        case 8: return launch_t<S, 8>(l, s);
+        case 16: return launch_t<S, 16>(l, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <typename S, int TY>
+int occ_t() {
+    int n = 0;
+    cudaFuncSetAttribute(step_kernel<S, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, Geo<TY>::SMEM);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<S, TY>, Geo<TY>::NTH, Geo<TY>::SMEM) !=
+        cudaSuccess)
+        return 0;
+    return n;
+}
+template <typename S>
+int occ_s(int ty) {
+    switch (ty) {
+        case 4: return occ_t<S, 4>();
+        case 8: return occ_t<S, 8>();
+        case 16: return occ_t<S, 16>();
+        default: return 0;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, cudaStream_t s) {
+    switch (storage) {
+        case MRLBM_STORAGE_F32: return launch_s<float>(l, tile_y, s);
+        case MRLBM_STORAGE_F16: return launch_s<__half>(l, tile_y, s);
+        case MRLBM_STORAGE_BF16: return launch_s<__nv_bfloat16>(l, tile_y, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_diag_finalize(const double *part, int n, double *out, cudaStream_t s) {
+    diag_finalize_kernel<<<1, 256, 0, s>>>(part, n, out);
+    return cudaGetLastError();
+}
+
+int step_kernel_smem_bytes(int tile_y) {
+    switch (tile_y) {
+        case 4: return Geo<4>::SMEM;
+        case 8: return Geo<8>::SMEM;
+        case 16: return Geo<16>::SMEM;
+        default: return 0;
+    }
+}
+
+int step_kernel_max_ctas_per_sm(int storage, int tile_y) {
+    switch (storage) {
+        case MRLBM_STORAGE_F32: return occ_s<float>(tile_y);
+        case MRLBM_STORAGE_F16: return occ_s<__half>(tile_y);
+        case MRLBM_STORAGE_BF16: return occ_s<__nv_bfloat16>(tile_y);
+        default: return 0;
+    }
+}
+
+}  // namespace mrlbm

@@ -1,0 +1,183 @@
+"""Python mirror of the reference's case / simulation interface over the C ABI.
+
+The reference selects a case at compile time (MRLBM_3D/src/config.h:8), fills a `struct Case`
+hook table (MRLBM_3D/src/common/globalStructs.cuh:46-62) and runs
+``streaming -> boundary_treatment -> post_streaming -> collision -> post_collision ->
+post_step`` per iteration (MRLBM_3D/src/main.cu:21-35).  Here a :class:`Simulation` owns one
+libmrlbm handle; one ``step`` runs that whole chain on the GPU, and the host-side hooks
+(``post_process_step``, ``write_output``) are plain Python callables run between steps at the
+reference's cadences.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Callable, Optional, Sequence
+
+import numpy as np
+
+from . import native as N
+
+
+@dataclass
+class Case:
+    """A case: the descriptor plus optional host hooks (the reference's `struct Case`)."""
+
+    desc: N.CaseDesc
+    name: str = "case"
+    init_kind: int = N.INIT_REFERENCE_NOISE
+    init_params: Sequence[float] = ()
+    post_process_step: Optional[Callable[["Simulation", int], None]] = None
+    write_output: Optional[Callable[["Simulation", int], None]] = None
+    finalize: Optional[Callable[["Simulation"], None]] = None
+    extra: dict = field(default_factory=dict)
+
+
+class Simulation:
+    """One MR-LBM case resident on the current CUDA device."""
+
+    def __init__(self, case: Case | N.CaseDesc, init: bool = True, host_only: bool = False):
+        if isinstance(case, N.CaseDesc):
+            case = Case(case)
+        self.case = case
+        L = N.lib()
+        h = C.c_void_p()
+        desc = N.CaseDesc.from_buffer_copy(case.desc)
+        create = L.mrlbm_create_host if host_only else L.mrlbm_create
+        N.check(create(C.byref(desc), C.byref(h)))
+        if host_only:
+            init = False
+        self._h = h
+        self.desc = desc
+        self.info = self.get_info()
+        self.n = int(self.info.n_nodes)
+        self.shape = (self.info.nz, self.info.ny, self.info.nx)
+        if init:
+            self.init(case.init_kind, case.init_params)
+
+    # ---- lifecycle ----------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            N.lib().mrlbm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _ck(self, rc):
+        return N.check(rc, self._h)
+
+    def get_info(self) -> N.Info:
+        info = N.Info()
+        self._ck(N.lib().mrlbm_get_info(self._h, C.byref(info)))
+        return info
+
+    def set_stream(self, stream_ptr: int | None):
+        self._ck(N.lib().mrlbm_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    # ---- time stepping ------------------------------------------------------------------
+    def init(self, kind: int = N.INIT_REFERENCE_NOISE, params: Sequence[float] = ()):
+        arr = (C.c_double * max(1, len(params)))(*params)
+        self._ck(N.lib().mrlbm_init(self._h, kind, arr, len(params)))
+
+    def step(self, n: int = 1):
+        self._ck(N.lib().mrlbm_step(self._h, int(n)))
+
+    def set_sampling(self, force_every: int = 0, diag_every: int = 0):
+        self._ck(N.lib().mrlbm_set_sampling(self._h, int(force_every), int(diag_every)))
+
+    def sync(self):
+        self._ck(N.lib().mrlbm_sync(self._h))
+
+    def run(self, max_iter: int, macr_save: int = 0, stat_start: int = 0, stat_end: int = -1):
+        """The reference's main loop: iterations start..max_iter inclusive (main.cu:21)."""
+        for it in range(0, max_iter + 1):
+            self.step(1)
+            if self.case.post_process_step and stat_start <= it and (stat_end < 0 or it <= stat_end):
+                self.case.post_process_step(self, it)
+            if self.case.write_output and macr_save and it % macr_save == 0:
+                self.case.write_output(self, it)
+        if self.case.finalize:
+            self.case.finalize(self)
+
+    # ---- fields -----------------------------------------------------------------------------
+    def moments(self, fields="all", layout: int = N.LAYOUT_LEXICOGRAPHIC, out: np.ndarray | None = None) -> np.ndarray:
+        """FP32 moments, shape (n_fields, nz, ny, nx) for the lexicographic layout."""
+        mask = N.field_mask(fields)
+        nf = bin(mask).count("1")
+        if out is None:
+            out = np.empty((nf, self.n), dtype=np.float32)
+        self._ck(N.lib().mrlbm_get_moments(self._h, mask, layout, out.ctypes.data_as(C.c_void_p), out.size))
+        if layout == N.LAYOUT_LEXICOGRAPHIC:
+            return out.reshape((nf,) + self.shape)
+        return out.reshape(nf, self.n)
+
+    def set_moments(self, values: np.ndarray, fields="all", layout: int = N.LAYOUT_LEXICOGRAPHIC):
+        mask = N.field_mask(fields)
+        v = N.as_f32(values)
+        self._ck(N.lib().mrlbm_set_moments(self._h, mask, layout, v.ctypes.data_as(C.c_void_p), v.size))
+
+    def node_types(self, layout: int = N.LAYOUT_LEXICOGRAPHIC) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.uint32)
+        self._ck(N.lib().mrlbm_get_node_types(self._h, layout, out.ctypes.data_as(C.c_void_p), out.size))
+        return out
+
+    def boundary(self, wall: int = 0, layout: int = N.LAYOUT_LEXICOGRAPHIC) -> dict:
+        """Boundary arrays of a curved wall: lists, normals, wall distances, direction masks."""
+        nb = int(self.info.nb[wall])
+        nbf = int(self.info.nb_fluid[wall])
+        L = N.lib()
+        res = {}
+        spec = [("list", N.BND_LIST, np.int64, nb), ("nx", N.BND_NORMAL_X, np.float32, nb),
+                ("ny", N.BND_NORMAL_Y, np.float32, nb), ("delta", N.BND_DELTA, np.float32, nb),
+                ("in_mask", N.BND_IN_MASK, np.uint32, nb), ("out_mask", N.BND_OUT_MASK, np.uint32, nb),
+                ("fluid_list", N.BND_FLUID_LIST, np.int64, nbf), ("tag_in_mask", N.BND_TAG_IN_MASK, np.uint32, 256),
+                ("tag_out_mask", N.BND_TAG_OUT_MASK, np.uint32, 256)]
+        for name, what, dt, n in spec:
+            a = np.zeros(max(n, 1), dtype=dt)
+            self._ck(L.mrlbm_get_boundary(self._h, wall, what, layout, a.ctypes.data_as(C.c_void_p), a.size))
+            res[name] = a[:n]
+        return res
+
+    # ---- statistics -------------------------------------------------------------------------
+    def forces(self, step: int = -1) -> np.ndarray:
+        """(2 walls, 5) array: Fx, Fy, Fz, mass flux, torque_z of one sampled step."""
+        out = np.zeros(10, dtype=np.float64)
+        self._ck(N.lib().mrlbm_get_forces(self._h, int(step), out.ctypes.data_as(C.c_void_p)))
+        return out.reshape(2, 5)
+
+    def force_history(self, max_steps: int = 1 << 16):
+        steps = np.zeros(max_steps, dtype=np.int64)
+        f = np.zeros((max_steps, 10), dtype=np.float64)
+        n = C.c_int32()
+        self._ck(N.lib().mrlbm_get_force_history(self._h, max_steps, steps.ctypes.data_as(C.c_void_p),
+                                                  f.ctypes.data_as(C.c_void_p), C.byref(n)))
+        return steps[: n.value], f[: n.value].reshape(-1, 2, 5)
+
+    def diagnostics(self, max_steps: int = 1 << 16):
+        """Sampled (step, mass, kinetic energy) over non-solid nodes, FP64."""
+        steps = np.zeros(max_steps, dtype=np.int64)
+        v = np.zeros((max_steps, 2), dtype=np.float64)
+        n = C.c_int32()
+        self._ck(N.lib().mrlbm_get_diagnostics(self._h, max_steps, steps.ctypes.data_as(C.c_void_p),
+                                                v.ctypes.data_as(C.c_void_p), C.byref(n)))
+        return steps[: n.value], v[: n.value]
+
+    # ---- files ------------------------------------------------------------------------------
+    def checkpoint_save(self, path: str):
+        self._ck(N.lib().mrlbm_checkpoint_save(self._h, str(path).encode()))
+
+    def checkpoint_load(self, path: str):
+        self._ck(N.lib().mrlbm_checkpoint_load(self._h, str(path).encode()))
+
+    def write_vti(self, path: str):
+        self._ck(N.lib().mrlbm_write_vti(self._h, str(path).encode()))

@@ -1,0 +1,72 @@
+"""Generate the golden fixtures under tests/golden/ from the reference's own code.
+
+ref_cylinder_geometry.npz — output of the reference's host node classification for its
+shipped cylinder case (336 x 144 x 48, D = 16, Re = 100, periodic y and z), produced by
+oracle/_ref/ref_geometry (oracle/ref_harness/ref_geometry.cu compiled from the reference
+sources by oracle/build_ref.py).  Index arrays are converted from the reference's tiled
+IDX_BLOCK order to lexicographic x + NX (y + NY z); the full node-type array is stored
+lexicographic too.
+
+Run from the repository root where the reference tree is mounted:
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle.build_ref import build_ref_geometry  # noqa: E402
+
+
+def tiled_to_lex(idx: np.ndarray, nx: int, ny: int, nz: int) -> np.ndarray:
+    """Inverse of the reference IDX_BLOCK (core/index.cuh:11-28, GlobalIndexToXYZ :86-111)."""
+    idx = idx.astype(np.int64)
+    gx, gy = nx // 8, ny // 8
+    block, thread = idx // 256, idx % 256
+    bx, by, bz = block % gx, (block // gx) % gy, block // (gx * gy)
+    tx, ty, tz = thread % 8, (thread // 8) % 8, thread // 64
+    x, y, z = bx * 8 + tx, by * 8 + ty, bz * 4 + tz
+    return x + nx * (y + ny * z)
+
+
+def make_geometry(out: Path):
+    exe = build_ref_geometry()
+    if exe is None:
+        raise SystemExit("reference tree not present: cannot regenerate")
+    with tempfile.TemporaryDirectory() as td:
+        subprocess.run([str(exe), td], check=True, capture_output=True)
+        d = Path(td)
+        rd = lambda name, dt: np.fromfile(d / name, dtype=dt)  # noqa: E731
+        meta = rd("meta.i32", np.int32)
+        fmeta = rd("meta.f32", np.float32)
+        nx, ny, nz, nb, nbf = (int(v) for v in meta[:5])
+        types_tiled = rd("node_type_tiled.u32", np.uint32)
+        lex = tiled_to_lex(np.arange(nx * ny * nz), nx, ny, nz)
+        types = np.empty_like(types_tiled)
+        types[lex] = types_tiled
+        np.savez_compressed(
+            out,
+            shape=np.array([nx, ny, nz], dtype=np.int32),
+            nb=np.int32(nb), nb_fluid=np.int32(nbf),
+            xc=fmeta[0], yc=fmeta[1], d_wall=fmeta[2], omega=fmeta[3],
+            node_types=types,
+            boundary_list=tiled_to_lex(rd("boundary_list_tiled.u64", np.uint64), nx, ny, nz),
+            unit_nx=rd("unit_nx.f32", np.float32), unit_ny=rd("unit_ny.f32", np.float32),
+            delta=rd("delta_w.f32", np.float32),
+            in_mask=rd("in_mask.u32", np.uint32), out_mask=rd("out_mask.u32", np.uint32),
+            fluid_list=tiled_to_lex(rd("bcfluid_list_tiled.u64", np.uint64), nx, ny, nz),
+            tag_in_mask=rd("tag_in_mask.u32", np.uint32), tag_out_mask=rd("tag_out_mask.u32", np.uint32),
+        )
+
+
+if __name__ == "__main__":
+    here = Path(__file__).resolve().parent
+    make_geometry(here / "ref_cylinder_geometry.npz")
+    print("wrote", here / "ref_cylinder_geometry.npz")

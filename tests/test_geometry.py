@@ -1,0 +1,84 @@
+"""Node classification: the product's and the oracle's restatements against the reference's
+own host code (golden fixture from tests/golden/make_golden.py), and against each other on
+the benchmark geometries."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+KEYS = [("list", "boundary_list"), ("nx", "unit_nx"), ("ny", "unit_ny"), ("delta", "delta"),
+        ("in_mask", "in_mask"), ("out_mask", "out_mask"), ("fluid_list", "fluid_list"),
+        ("tag_in_mask", "tag_in_mask"), ("tag_out_mask", "tag_out_mask")]
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(GOLDEN / "ref_cylinder_geometry.npz")
+
+
+def test_golden_fixture_is_consistent(golden):
+    t = golden["node_types"]
+    cls = t >> 20
+    assert int(golden["nb"]) == int((cls == 2).sum()) == len(golden["boundary_list"])
+    assert int(golden["nb_fluid"]) == int((cls == 4).sum()) == len(golden["fluid_list"])
+    # boundary indices are assigned in list order (cylinder_helpers.cuh:116-132)
+    assert np.array_equal(t[golden["boundary_list"]] & 0xFFFFF, np.arange(int(golden["nb"])))
+
+
+def test_product_geometry_matches_reference(built, golden):
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    s = Simulation(cases.reference_cylinder(), host_only=True)
+    assert np.array_equal(s.node_types(), golden["node_types"])
+    b = s.boundary(0)
+    for k, g in KEYS:
+        assert np.array_equal(b[k], golden[g]), k
+    assert s.info.omega == golden["omega"]
+
+
+def test_oracle_geometry_matches_reference(built, golden):
+    import oracle
+    from mrlbm_3d_cuda_gb300 import cases
+    o = oracle.Oracle(cases.reference_cylinder(), 64)
+    assert np.array_equal(o.node_types(), golden["node_types"])
+    b = o.boundary(0)
+    for k, g in KEYS:
+        assert np.array_equal(b[k], golden[g]), k
+
+
+def test_reference_tiled_layout_round_trip(built, golden):
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    from tests.golden.make_golden import tiled_to_lex
+    s = Simulation(cases.reference_cylinder(), host_only=True)
+    tiled = s.node_types(N.LAYOUT_REF_TILED)
+    nx, ny, nz = (int(v) for v in golden["shape"])
+    lex = tiled_to_lex(np.arange(nx * ny * nz), nx, ny, nz)
+    back = np.empty_like(tiled)
+    back[lex] = tiled
+    assert np.array_equal(back, golden["node_types"])
+
+
+@pytest.mark.parametrize("name", ["c1", "annulus_small", "annulus_ref", "channel_staircase", "cylinder_box_walls"])
+def test_product_and_oracle_classify_alike(built, name):
+    import oracle
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    desc = {
+        "c1": lambda: cases.c1_cylinder(),
+        "annulus_small": lambda: cases.annulus(48, 48, 8, 8.0, 20.0, 0.05, 50.0),
+        "annulus_ref": lambda: cases.reference_annulus(),
+        "channel_staircase": lambda: cases.cylinder_channel(64, 32, 8, 8, 20.0, 15.5, 0.05, 40.0, triangular=False),
+        "cylinder_box_walls": lambda: cases.cylinder_channel(64, 40, 12, 10, 24.3, 19.7, 0.05, 60.0),
+    }[name]()
+    s = Simulation(desc, host_only=True)
+    o = oracle.Oracle(desc, 64)
+    assert np.array_equal(s.node_types(), o.node_types())
+    for w in range(2 if desc.geometry == 2 else 1):
+        bs, bo = s.boundary(w), o.boundary(w)
+        for k, _ in KEYS:
+            assert np.array_equal(bs[k], bo[k]), (w, k)
+    cls = s.node_types() >> 20
+    assert (cls == 2).any()
+    if desc.geometry == 2:
+        assert (cls == 3).any()
