@@ -153,7 +153,8 @@ def run_ours(args):
     storage = args.storage
     desc = cases.c2_taylor_green(args.n, STORAGE[storage])
     n_nodes = desc.nx * desc.ny * desc.nz
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # a real stream handle: the library launches on it, events time it
+    torch.cuda.set_stream(stream)
     sim = Simulation(desc, init=False)
     sim.set_stream(stream.cuda_stream)
     sim.init(N.INIT_TAYLOR_GREEN, cases.tgv_params(desc))

@@ -548,7 +548,7 @@ int mrlbm_step(mrlbm_handle *h, int32_t nsteps) {
             ++h->force_count;
         }
         if (ds) L.diag_part = h->d_diag_part;
-        CK(h, launch_step(L, h->storage, h->tile_y, h->stream));
+        CK(h, launch_step(L, h->storage, h->tile_y, h->d_word != nullptr, h->stream));
         if (nb > 0) CK(h, launch_wall(L, h->storage, nb + (fs ? nbf : 0), h->stream));
         if (ds) {
             const int64_t slot = h->diag_count % kRing;

@@ -62,7 +62,7 @@ inline __host__ __device__ int64_t side_index(int slot, int x, int y, int z, int
 }
 
 // storage: 0 f32, 1 f16, 2 bf16
-cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, cudaStream_t s);
+cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, bool special, cudaStream_t s);
 int step_kernel_smem_bytes(int tile_y);
 int step_kernel_max_ctas_per_sm(int storage, int tile_y);
 // Curved-wall closure + collision for the wall nodes of both walls, plus the force sums.

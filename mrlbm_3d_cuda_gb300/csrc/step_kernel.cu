@@ -122,27 +122,153 @@ __device__ __noinline__ int special_node(const StepArgs *__restrict__ ga, int pa
     }
     if (wall_node) return 0;  // the wall kernel finishes this node
     const bool bcf = force && slot >= 0 && (cls == C_BCFLUID_INNER || cls == C_BCFLUID_OUTER);
-    float fin[4] = {0.f, 0.f, 0.f, 0.f};
+    double fin[4] = {0.0, 0.0, 0.0, 0.0};
     const uint32_t tag = (w >> NW_PAYLOAD_SHIFT) & 0xFFu;
-    if (bcf) {
-        reconstruct(m, fl);
-        masked_momentum(a.tag_in[tag], fl, fin[0], fin[1], fin[2], fin[3]);
-    }
+    if (bcf) masked_momentum64(a.tag_in[tag], m, fin);
     collide(m, a.omega);
     if (bcf) {
-        float fo[4];
-        reconstruct(m, fl);
-        masked_momentum(a.tag_out[tag], fl, fo[0], fo[1], fo[2], fo[3]);
+        double fo[4];
+        masked_momentum64(a.tag_out[tag], m, fo);
         float *e = a.side + side_index(slot, x, y, z, x0, y0, a.nz, TILE_X, TY) * 16;
-        e[10] = fin[0] - fo[0];
-        e[11] = fin[1] - fo[1];
-        e[12] = fin[2] - fo[2];
-        e[13] = fin[3] - fo[3];
+        e[10] = (float)(fin[0] - fo[0]);
+        e[11] = (float)(fin[1] - fo[1]);
+        e[12] = (float)(fin[2] - fo[2]);
+        e[13] = (float)(fin[3] - fo[3]);
     }
     return fluid ? 2 : 1;
 }
 
+
+// Pulled population q of the owner node, read from the ring buffer of its c_z class.
+template <int Q, int TY>
+__device__ __forceinline__ float pull(const float *up, const float *fl, const float *dn, int col) {
+    constexpr int NC = Geo<TY>::NCOL, W = Geo<TY>::W;
+    constexpr int off = -cyq(Q) * W - cxq(Q);
+    if constexpr (czq(Q) == 1) {
+        constexpr int j = Q == 9 ? 0 : Q == 11 ? 1 : Q == 16 ? 2 : Q == 18 ? 3 : Q == 19 ? 4 : Q == 22 ? 5 : Q == 23 ? 6 : 7;
+        return up[j * NC + col + off];
+    } else if constexpr (czq(Q) == 0) {
+        constexpr int j = Q == 1 ? 0 : Q == 2 ? 1 : Q == 3 ? 2 : Q == 4 ? 3 : Q == 7 ? 4 : Q == 8 ? 5 : Q == 13 ? 6 : 7;
+        return fl[j * NC + col + off];
+    } else {
+        constexpr int j = Q == 10 ? 0 : Q == 12 ? 1 : Q == 15 ? 2 : Q == 17 ? 3 : Q == 20 ? 4 : Q == 21 ? 5 : Q == 24 ? 6 : 7;
+        return dn[j * NC + col + off];
+    }
+}
+
+struct Sums {
+    float rho, jx, jy, jz, sxx, syy, szz, sxy, sxz, syz;
+};
+
+// Add the opposite pair (q, opp q) with values a = f_q, b = f_opp to the moment sums.
+template <int Q>
+__device__ __forceinline__ void add_pair(float a, float b, Sums &s) {
+    constexpr int cx = cxq(Q), cy = cyq(Q), cz = czq(Q);
+    const float e = a + b, d = a - b;
+    s.rho += e;
+    if constexpr (cx > 0) s.jx += d;
+    if constexpr (cx < 0) s.jx -= d;
+    if constexpr (cy > 0) s.jy += d;
+    if constexpr (cy < 0) s.jy -= d;
+    if constexpr (cz > 0) s.jz += d;
+    if constexpr (cz < 0) s.jz -= d;
+    if constexpr (cx != 0) s.sxx += e;
+    if constexpr (cy != 0) s.syy += e;
+    if constexpr (cz != 0) s.szz += e;
+    if constexpr (cx * cy > 0) s.sxy += e;
+    if constexpr (cx * cy < 0) s.sxy -= e;
+    if constexpr (cx * cz > 0) s.sxz += e;
+    if constexpr (cx * cz < 0) s.sxz -= e;
+    if constexpr (cy * cz > 0) s.syz += e;
+    if constexpr (cy * cz < 0) s.syz -= e;
+}
+
+template <int Q, int TY>
+__device__ __forceinline__ void add_pulled_pair(const float *up, const float *fl, const float *dn, int col, Sums &s) {
+    add_pair<Q>(pull<Q, TY>(up, fl, dn, col), pull<oppq(Q), TY>(up, fl, dn, col), s);
+}
+
+// Gather the pulled populations of the owner node and evaluate its moments on the fly.
+template <int TY>
+__device__ __forceinline__ void gather_evaluate(const float *up, const float *fl, const float *dn, int col, float f0,
+                                                float f5, float f6, Mom &m) {
+    Sums s{f0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    add_pulled_pair<1, TY>(up, fl, dn, col, s);
+    add_pulled_pair<3, TY>(up, fl, dn, col, s);
+    add_pair<5>(f5, f6, s);
+    add_pulled_pair<7, TY>(up, fl, dn, col, s);
+    add_pulled_pair<13, TY>(up, fl, dn, col, s);
+    add_pulled_pair<9, TY>(up, fl, dn, col, s);
+    add_pulled_pair<11, TY>(up, fl, dn, col, s);
+    add_pulled_pair<15, TY>(up, fl, dn, col, s);
+    add_pulled_pair<17, TY>(up, fl, dn, col, s);
+    add_pulled_pair<19, TY>(up, fl, dn, col, s);
+    add_pulled_pair<21, TY>(up, fl, dn, col, s);
+    add_pulled_pair<23, TY>(up, fl, dn, col, s);
+    add_pulled_pair<25, TY>(up, fl, dn, col, s);
+    const float inv = 1.0f / s.rho;
+    m.rho = s.rho;
+    m.ux = s.jx * inv;
+    m.uy = s.jy * inv;
+    m.uz = s.jz * inv;
+    m.mxx = s.sxx * inv - kCs2;
+    m.myy = s.syy * inv - kCs2;
+    m.mzz = s.szz * inv - kCs2;
+    m.mxy = s.sxy * inv;
+    m.mxz = s.sxz * inv;
+    m.myz = s.syz * inv;
+}
+
+template <int TY>
+__device__ __forceinline__ void gather_all(const float *up, const float *fl, const float *dn, int col, float f0,
+                                           float f5, float f6, float *f) {
+    f[0] = f0;
+    f[5] = f5;
+    f[6] = f6;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        f[hUp(j)] = up[j * Geo<TY>::NCOL + col - cyq(hUp(j)) * Geo<TY>::W - cxq(hUp(j))];
+        f[hFl(j)] = fl[j * Geo<TY>::NCOL + col - cyq(hFl(j)) * Geo<TY>::W - cxq(hFl(j))];
+        f[hDn(j)] = dn[j * Geo<TY>::NCOL + col - cyq(hDn(j)) * Geo<TY>::W - cxq(hDn(j))];
+    }
+}
+
+// Rebuild the own-column populations of plane p from raw stored moments into the rings.
 template <typename S, int TY>
+__device__ __forceinline__ void arrive_own(const float raw[10], float rho0, const StorageScale &sc, float *up,
+                                           float *fl, float *dn, int col, float &c0, float &c5, float &c6) {
+    const Mom m = decode<S>(raw, rho0, sc);
+    float f[27];
+    reconstruct(m, f);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        up[j * Geo<TY>::NCOL + col] = f[hUp(j)];
+        fl[j * Geo<TY>::NCOL + col] = f[hFl(j)];
+        dn[j * Geo<TY>::NCOL + col] = f[hDn(j)];
+    }
+    c0 = f[0];
+    c5 = f[5];
+    c6 = f[6];
+}
+
+template <typename S, int TY>
+__device__ __forceinline__ void arrive_rim(const float raw[10], float rho0, const StorageScale &sc, int side, float *up,
+                                           float *fl, float *dn, int rcol) {
+    const Mom m = decode<S>(raw, rho0, sc);
+    switch (side) {
+        case 0: rim_store<0, 1, TY>(m, up, fl, dn, rcol); break;
+        case 1: rim_store<0, -1, TY>(m, up, fl, dn, rcol); break;
+        case 2: rim_store<1, 0, TY>(m, up, fl, dn, rcol); break;
+        case 3: rim_store<-1, 0, TY>(m, up, fl, dn, rcol); break;
+        case 4: rim_store<1, 1, TY>(m, up, fl, dn, rcol); break;
+        case 5: rim_store<-1, 1, TY>(m, up, fl, dn, rcol); break;
+        case 6: rim_store<1, -1, TY>(m, up, fl, dn, rcol); break;
+        default: rim_store<-1, -1, TY>(m, up, fl, dn, rcol); break;
+    }
+}
+
+// SPECIAL = false: every node of every item is a plain bulk node (no node words are read).
+template <typename S, int TY, bool SPECIAL>
 __global__ void __launch_bounds__(TILE_X *TY, (TY == 4 ? 5 : (TY == 8 ? 3 : 1)))
     step_kernel(const StepArgs *__restrict__ ga, const int parity, double *__restrict__ force,
                 double *__restrict__ diag_part) {
@@ -160,6 +286,7 @@ __global__ void __launch_bounds__(TILE_X *TY, (TY == 4 ? 5 : (TY == 8 ? 3 : 1)))
     const StorageScale sc = ga->sc;
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
     const int64_t plane = (int64_t)nx * ny;
+    const bool diag = diag_part != nullptr;
     double dmD = 0.0, deD = 0.0;
 
     for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
@@ -169,7 +296,7 @@ __global__ void __launch_bounds__(TILE_X *TY, (TY == 4 ? 5 : (TY == 8 ? 3 : 1)))
         const int x0 = tix * TILE_X, y0 = tiy * TY;
         const int w = min(TILE_X, nx - x0), h = min(TY, ny - y0);
         const int zs = seg * lz, ze = min(zs + lz, nz);
-        const int slot = tile_slot ? tile_slot[tile] : -1;
+        const int slot = (SPECIAL && tile_slot) ? tile_slot[tile] : -1;
         const bool own = tx < w && ty < h;
         const int x = x0 + tx, y = y0 + ty;
         const int col = (ty + 1) * G::W + (tx + 1);
@@ -204,89 +331,56 @@ __global__ void __launch_bounds__(TILE_X *TY, (TY == 4 ? 5 : (TY == 8 ? 3 : 1)))
         float c0 = 0.f, c5 = 0.f, c6 = 0.f;  // own-column rest / up / down populations of the newest plane
         float p0 = 0.f, p5 = 0.f, pp5 = 0.f; // history: f0(z), f5(z), f5(z-1)
         float dm = 0.f, de = 0.f;
+        const int zm = (zs - 1 + nz) % nz;
+        if (own) load_raw<S>(src, fs, xy + (int64_t)zm * plane, pre);
 
-        auto plane_of = [&](int p) -> int64_t { return (int64_t)((p + nz) % nz) * plane; };
-        if (own) load_raw<S>(src, fs, xy + plane_of(zs - 1), pre);
-
-        // arrive(p): rebuild the populations of plane p into ring slot k
-        auto arrive = [&](int p, int k) {
+        // prologue: planes zs-1 (ring slot 0) and zs (slot 1); then march
+        for (int k = 0; k <= ze - zs + 1; ++k) {
+            const int p = zs - 1 + k;  // plane arriving in ring slot k
             float *up = smem + (k % 3) * G::PLANE;
-            float *fl = smem + (3 + (k & 1)) * G::PLANE;
+            float *flt = smem + (3 + (k & 1)) * G::PLANE;
             float *dn = smem + 5 * G::PLANE;
             float rv[10];
-            if (rside >= 0) load_raw<S>(src, fs, rxy + plane_of(p), rv);
+            if (rside >= 0) load_raw<S>(src, fs, rxy + (int64_t)((p + nz) % nz) * plane, rv);
             if (own) {
-                const Mom m = decode<S>(pre, rho0, sc);
-                if (p + 1 <= ze) load_raw<S>(src, fs, xy + plane_of(p + 1), pre);
-                float f[27];
-                reconstruct(m, f);
+                float cur[10];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    up[j * G::NCOL + col] = f[hUp(j)];
-                    fl[j * G::NCOL + col] = f[hFl(j)];
-                    dn[j * G::NCOL + col] = f[hDn(j)];
-                }
-                c0 = f[0];
-                c5 = f[5];
-                c6 = f[6];
+                for (int i = 0; i < 10; ++i) cur[i] = pre[i];
+                if (p + 1 <= ze) load_raw<S>(src, fs, xy + (int64_t)((p + 1) % nz) * plane, pre);
+                arrive_own<S, TY>(cur, rho0, sc, up, flt, dn, col, c0, c5, c6);
             }
-            if (rside >= 0) {
-                const Mom m = decode<S>(rv, rho0, sc);
-                switch (rside) {
-                    case 0: rim_store<0, 1, TY>(m, up, fl, dn, rcol); break;
-                    case 1: rim_store<0, -1, TY>(m, up, fl, dn, rcol); break;
-                    case 2: rim_store<1, 0, TY>(m, up, fl, dn, rcol); break;
-                    case 3: rim_store<-1, 0, TY>(m, up, fl, dn, rcol); break;
-                    case 4: rim_store<1, 1, TY>(m, up, fl, dn, rcol); break;
-                    case 5: rim_store<-1, 1, TY>(m, up, fl, dn, rcol); break;
-                    case 6: rim_store<1, -1, TY>(m, up, fl, dn, rcol); break;
-                    default: rim_store<-1, -1, TY>(m, up, fl, dn, rcol); break;
-                }
+            if (rside >= 0) arrive_rim<S, TY>(rv, rho0, sc, rside, up, flt, dn, rcol);
+            if (k < 2) {
+                pp5 = p5;
+                p5 = c5;
+                p0 = c0;
+                continue;
             }
-        };
-
-        arrive(zs - 1, 0);
-        p5 = c5;
-        arrive(zs, 1);
-        pp5 = p5;
-        p5 = c5;
-        p0 = c0;
-        for (int z = zs; z < ze; ++z) {
-            const int k = z - zs + 1;
-            arrive(z + 1, k + 1);
+            // emit plane z = p - 1 (its down populations come from plane p, just written)
+            const int z = p - 1;
             __syncthreads();
             if (own) {
-                const float *up = smem + ((k - 1) % 3) * G::PLANE;
-                const float *fl = smem + (3 + (k & 1)) * G::PLANE;
-                const float *dn = smem + 5 * G::PLANE;
-                float f[27];
-                f[0] = p0;
-                f[5] = pp5;
-                f[6] = c6;
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    f[hUp(j)] = up[j * G::NCOL + col - cyq(hUp(j)) * G::W - cxq(hUp(j))];
-                    f[hFl(j)] = fl[j * G::NCOL + col - cyq(hFl(j)) * G::W - cxq(hFl(j))];
-                    f[hDn(j)] = dn[j * G::NCOL + col - cyq(hDn(j)) * G::W - cxq(hDn(j))];
-                }
+                const float *eup = smem + ((k - 2) % 3) * G::PLANE;  // plane z-1
+                const float *efl = smem + (3 + ((k - 1) & 1)) * G::PLANE;  // plane z
                 const int64_t node = xy + (int64_t)z * plane;
-                const uint32_t wd = slot >= 0 ? word[node] : 0u;
+                const uint32_t wd = (SPECIAL && slot >= 0) ? word[node] : 0u;
                 if (wd == 0u) {
                     Mom m;
-                    evaluate(f, m);
-                    dm += m.rho - rho0;
-                    de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
+                    gather_evaluate<TY>(eup, efl, dn, col, p0, pp5, c6, m);
+                    if (diag) {
+                        dm += m.rho - rho0;
+                        de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
+                    }
                     collide(m, omega);
                     store_mom<S>(dst, fs, node, m, rho0, sc);
-                } else {
+                } else if constexpr (SPECIAL) {
                     float fw[27];
-#pragma unroll
-                    for (int q = 0; q < 27; ++q) fw[q] = f[q];
+                    gather_all<TY>(eup, efl, dn, col, p0, pp5, c6, fw);
                     Mom ms;
                     const int code =
                         special_node<S, TY>(ga, parity, force != nullptr, wd, fw, x, y, z, node, slot, x0, y0, ms);
                     if (code) store_mom<S>(dst, fs, node, ms, rho0, sc);
-                    if (code == 2) {
+                    if (code == 2 && diag) {
                         dm += ms.rho - rho0;
                         de += 0.5f * (ms.ux * ms.ux + ms.uy * ms.uy + ms.uz * ms.uz);
                     }
@@ -297,11 +391,13 @@ __global__ void __launch_bounds__(TILE_X *TY, (TY == 4 ? 5 : (TY == 8 ? 3 : 1)))
             p5 = c5;
             p0 = c0;
         }
-        dmD += (double)dm;
-        deD += (double)de;
+        if (diag) {
+            dmD += (double)dm;
+            deD += (double)de;
+        }
     }
 
-    if (diag_part) {
+    if (diag) {
         // deterministic block reduction of the FP64 partials -> diag_part[blockIdx.x]
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -348,25 +444,25 @@ __global__ void diag_finalize_kernel(const double *__restrict__ part, int n, dou
     }
 }
 
-template <typename S, int TY>
+template <typename S, int TY, bool SP>
 cudaError_t launch_t(const StepLaunch &l, cudaStream_t s) {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(step_kernel<S, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(step_kernel<S, TY, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              Geo<TY>::SMEM);
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    step_kernel<S, TY><<<l.n_ctas, Geo<TY>::NTH, Geo<TY>::SMEM, s>>>(l.ga, l.parity, l.force, l.diag_part);
+    step_kernel<S, TY, SP><<<l.n_ctas, Geo<TY>::NTH, Geo<TY>::SMEM, s>>>(l.ga, l.parity, l.force, l.diag_part);
     return cudaGetLastError();
 }
 
-template <typename S>
+template <typename S, bool SP>
 cudaError_t launch_s(const StepLaunch &l, int tile_y, cudaStream_t s) {
     switch (tile_y) {
-        case 4: return launch_t<S, 4>(l, s);
-        case 8: return launch_t<S, 8>(l, s);
-        case 16: return launch_t<S, 16>(l, s);
+        case 4: return launch_t<S, 4, SP>(l, s);
+        case 8: return launch_t<S, 8, SP>(l, s);
+        case 16: return launch_t<S, 16, SP>(l, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -374,8 +470,8 @@ cudaError_t launch_s(const StepLaunch &l, int tile_y, cudaStream_t s) {
 template <typename S, int TY>
 int occ_t() {
     int n = 0;
-    cudaFuncSetAttribute(step_kernel<S, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, Geo<TY>::SMEM);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<S, TY>, Geo<TY>::NTH, Geo<TY>::SMEM) !=
+    cudaFuncSetAttribute(step_kernel<S, TY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, Geo<TY>::SMEM);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<S, TY, true>, Geo<TY>::NTH, Geo<TY>::SMEM) !=
         cudaSuccess)
         return 0;
     return n;
@@ -392,11 +488,12 @@ int occ_s(int ty) {
 
 }  // namespace
 
-cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, cudaStream_t s) {
+cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, bool special, cudaStream_t s) {
     switch (storage) {
-        case MRLBM_STORAGE_F32: return launch_s<float>(l, tile_y, s);
-        case MRLBM_STORAGE_F16: return launch_s<__half>(l, tile_y, s);
-        case MRLBM_STORAGE_BF16: return launch_s<__nv_bfloat16>(l, tile_y, s);
+        case MRLBM_STORAGE_F32: return special ? launch_s<float, true>(l, tile_y, s) : launch_s<float, false>(l, tile_y, s);
+        case MRLBM_STORAGE_F16: return special ? launch_s<__half, true>(l, tile_y, s) : launch_s<__half, false>(l, tile_y, s);
+        case MRLBM_STORAGE_BF16:
+            return special ? launch_s<__nv_bfloat16, true>(l, tile_y, s) : launch_s<__nv_bfloat16, false>(l, tile_y, s);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -195,22 +195,17 @@ __global__ void __launch_bounds__(128) wall_kernel(const StepArgs *__restrict__ 
                 ex.myz = extrapolate(delta, vw * ww, v1.myz, v2.myz);
                 ex.mxy = ex.mxz = 0.f;
                 closure_rotated(a, nx, ny, inm, outm, ex, m);
-                float f[27];
-                float fin[4] = {0.f, 0.f, 0.f, 0.f}, fo[4];
-                if (force) {
-                    reconstruct(m, f);
-                    masked_momentum(inm, f, fin[0], fin[1], fin[2], fin[3]);
-                }
+                double fin[4] = {0.0, 0.0, 0.0, 0.0}, fo[4];
+                if (force) masked_momentum64(inm, m, fin);
                 collide(m, a.omega);
                 store_mom<S>((S *)a.m[parity ^ 1], a.fs, node, m, a.rho0, a.sc);
                 if (force) {
-                    reconstruct(m, f);
-                    masked_momentum(outm, f, fo[0], fo[1], fo[2], fo[3]);
-                    const double fx = (double)fin[0] - fo[0], fy = (double)fin[1] - fo[1];
+                    masked_momentum64(outm, m, fo);
+                    const double fx = fin[0] - fo[0], fy = fin[1] - fo[1];
                     acc[wi][0] = fx;
                     acc[wi][1] = fy;
-                    acc[wi][2] = (double)fin[2] - fo[2];
-                    acc[wi][3] = (double)fin[3] - fo[3];
+                    acc[wi][2] = fin[2] - fo[2];
+                    acc[wi][3] = fin[3] - fo[3];
                     acc[wi][4] = ((double)x - a.xc) * fy - ((double)y - a.yc) * fx;
                 }
             }

@@ -1,12 +1,15 @@
 """GPU parity: the CUDA solver (through the C ABI) against the oracle on the same inputs.
 
-Tolerance: per field, max |gpu - oracle| / max(|oracle|_inf, s_f) <= 1e-5 after N steps,
+Field metric (conftest.field_errors): per field, max |gpu - oracle| / max(|oracle|_inf, s_f)
 with s_f the magnitude of the quantity as the FP32 algorithm computes it (rho: 1, u: U,
-m_ab: cs2 = 1/3); see conftest.field_errors.  Forces: relative 5e-3 of |F| (the stated
-Cd / Cl tolerance), in practice far tighter."""
+m_ab: cs2 = 1/3).  Criteria, per field:
+  * strict:   <= 1e-5 against the FP32 oracle (reference arithmetic order) on short runs;
+  * rounding: on longer runs FP32 rounding of the reference's own arithmetic grows past
+    1e-5 in impulsively started flows, so the GPU must stay within max(1e-5, 2 x e32) of
+    the FP32 oracle and within max(1e-5, 1.5 x e32) of the FP64 oracle, where e32 is the
+    FP32 oracle's own distance from the FP64 oracle (the FP32 noise floor).
+Forces: relative 5e-3 of |F| (the stated Cd / Cl tolerance), in practice far tighter."""
 from __future__ import annotations
-
-import os
 
 import numpy as np
 import pytest
@@ -17,38 +20,67 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-5
 
 
-def run_pair(desc, steps, init_kind, params=(), forces=False, bits=32):
+def run_pair(desc, steps, init_kind, params=(), forces=False, fp64=True):
     import oracle
     from mrlbm_3d_cuda_gb300 import Simulation
     sim = Simulation(desc, init=False)
     sim.init(init_kind, params)
     if forces:
         sim.set_sampling(1, 0)
-    o = oracle.Oracle(desc, bits)
-    o.init(init_kind, params)
+    orc = {32: oracle.Oracle(desc, 32)}
+    if fp64:
+        orc[64] = oracle.Oracle(desc, 64)
+    for o in orc.values():
+        o.init(init_kind, params)
     # initial states agree exactly (same initialiser arithmetic)
-    g0 = sim.moments()
-    o0 = o.moments()
-    if bits == 32:
-        assert np.array_equal(g0.astype(np.float64), o0), "initial state differs"
-    for s in range(steps):
-        sim.step(1)
-        o.step(1, forces=forces and s == steps - 1)
+    assert np.array_equal(sim.moments().astype(np.float64), orc[32].moments()), "initial state differs"
+    sim.step(steps)
+    for o in orc.values():
+        if steps > 1:
+            o.step(steps - 1)
+        if steps > 0:
+            o.step(1, forces=forces)
     sim.sync()
-    res = {"gpu": sim.moments(), "oracle": o.moments(), "types": sim.node_types()}
+    res = {"gpu": sim.moments(), "oracle": orc[32].moments(), "types": sim.node_types()}
+    if fp64:
+        res["oracle64"] = orc[64].moments()
     if forces:
         res["gpu_f"] = sim.forces()
-        res["oracle_f"] = o.forces()
+        res["oracle_f"] = orc[32].forces()
+        if fp64:
+            res["oracle64_f"] = orc[64].forces()
     sim.close()
-    o.close()
+    for o in orc.values():
+        o.close()
     return res
 
 
-def assert_fields(res, u_ref, tol=TOL):
-    err = field_errors(res["gpu"], res["oracle"], u_ref)
+def assert_fields(res, u_ref, strict=False):
     assert np.isfinite(res["gpu"]).all()
-    assert err[:, 0].max() < tol, "\n" + np.array2string(err, precision=3)
-    return err
+    e_g32 = field_errors(res["gpu"], res["oracle"], u_ref)[:, 0]
+    if strict or "oracle64" not in res:
+        assert e_g32.max() < TOL, "\n" + np.array2string(e_g32, precision=3)
+        return e_g32
+    e_3264 = field_errors(res["oracle"], res["oracle64"], u_ref)[:, 0]
+    e_g64 = field_errors(res["gpu"], res["oracle64"], u_ref)[:, 0]
+    table = "\n gpu-o32 " + np.array2string(e_g32, precision=2) + "\n o32-o64 " + \
+            np.array2string(e_3264, precision=2) + "\n gpu-o64 " + np.array2string(e_g64, precision=2)
+    assert (e_g32 <= np.maximum(TOL, 2.0 * e_3264)).all(), table
+    assert (e_g64 <= np.maximum(TOL, 1.5 * e_3264)).all(), table
+    return e_g32
+
+
+def assert_forces(res, wall: int, comps=(0, 1, 4), rel=5e-3):
+    """GPU force (FP64 integration) vs the FP64 oracle: within 5e-3 of the force scale, or
+    within 3x the FP32 oracle's own distance from the FP64 oracle.  A force is one scalar
+    sum of per-node in - out momentum differences that cancel most digits, so its FP32
+    noise is a single random draw: the factor is wider than for the field maxima."""
+    fg, f32, f64 = res["gpu_f"][wall], res["oracle_f"][wall], res["oracle64_f"][wall]
+    scale = np.abs(f64[[0, 1]]).max()
+    for k in comps:
+        ref = abs(f64[k]) if k != 4 else max(abs(f64[4]), 1e-12)
+        bound = max(rel * max(ref, rel * scale if k in (0, 1) else ref), 3.0 * abs(f32[k] - f64[k]))
+        assert abs(fg[k] - f64[k]) <= bound, (wall, k, fg, f32, f64)
 
 
 def test_reference_noise_initialiser_is_bitwise(cuda_device):
@@ -63,7 +95,7 @@ def test_taylor_green_periodic(cuda_device):
     from mrlbm_3d_cuda_gb300 import native as N
     desc = cases.periodic_box(32, u0=0.05, re=400.0)
     res = run_pair(desc, 30, N.INIT_TAYLOR_GREEN, cases.tgv_params(desc))
-    assert_fields(res, 0.05)
+    assert_fields(res, 0.05, strict=True)
 
 
 def test_non_multiple_of_tile_grid(cuda_device):
@@ -72,7 +104,15 @@ def test_non_multiple_of_tile_grid(cuda_device):
     from mrlbm_3d_cuda_gb300 import native as N
     desc = cases.periodic_box(40, 24, 12, u0=0.04, re=100.0)
     res = run_pair(desc, 12, N.INIT_NOISY_UNIFORM, (0.03, 0.01, -0.02, 0.3, 11))
-    assert_fields(res, 0.05)
+    assert_fields(res, 0.05, strict=True)
+
+
+def test_channel_short_run_strict(cuda_device):
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    desc = cases.cylinder_channel(64, 40, 12, 10, 24.3, 19.7, 0.05, 60.0)
+    res = run_pair(desc, 6, N.INIT_REST, forces=True, fp64=False)
+    assert_fields(res, 0.05, strict=True)
 
 
 def test_channel_with_cylinder_walls_and_edges(cuda_device):
@@ -82,31 +122,30 @@ def test_channel_with_cylinder_walls_and_edges(cuda_device):
     desc = cases.cylinder_channel(64, 40, 12, 10, 24.3, 19.7, 0.05, 60.0)
     res = run_pair(desc, 40, N.INIT_REST, forces=True)
     assert_fields(res, 0.05)
-    fg, fo = res["gpu_f"][0], res["oracle_f"][0]
-    assert np.abs(fg[:3] - fo[:3]).max() <= 5e-3 * np.abs(fo[:3]).max()
-    assert abs(fg[4] - fo[4]) <= 5e-3 * max(abs(fo[4]), 1e-3 * np.abs(fo[:2]).max())
+    assert_forces(res, 0, comps=(0, 1, 3, 4))
 
 
-def test_reference_cylinder_case(cuda_device):
+@pytest.mark.parametrize("steps", [8, 160])
+def test_reference_cylinder_case(cuda_device, steps):
     """The reference's shipped case (convective outlet, periodic y) from its own initial
-    state, 8 steps."""
+    state; after ~125 steps the inlet pressure wave has reached the cylinder and the force
+    is no longer round-off."""
     from mrlbm_3d_cuda_gb300 import cases
     from mrlbm_3d_cuda_gb300 import native as N
-    res = run_pair(cases.reference_cylinder(), 8, N.INIT_REFERENCE_NOISE, forces=True)
+    res = run_pair(cases.reference_cylinder(), steps, N.INIT_REFERENCE_NOISE, forces=True)
     assert_fields(res, 0.1)
-    fg, fo = res["gpu_f"][0], res["oracle_f"][0]
-    assert np.abs(fg[:2] - fo[:2]).max() <= 5e-3 * np.abs(fo[:2]).max()
+    if steps > 125:
+        assert_forces(res, 0, comps=(0, 1))
 
 
 def test_annulus_two_walls(cuda_device):
     from mrlbm_3d_cuda_gb300 import cases
     from mrlbm_3d_cuda_gb300 import native as N
     desc = cases.annulus(48, 48, 8, 8.0, 20.0, 0.05, 50.0)
-    res = run_pair(desc, 30, N.INIT_REST, forces=True)
+    res = run_pair(desc, 200, N.INIT_REST, forces=True)
     assert_fields(res, 0.05)
-    fg, fo = res["gpu_f"], res["oracle_f"]
     for w in range(2):
-        assert abs(fg[w, 4] - fo[w, 4]) <= 5e-3 * abs(fo[w, 4]) + 1e-9
+        assert_forces(res, w, comps=(4,))
 
 
 def test_staircase_classification(cuda_device):
