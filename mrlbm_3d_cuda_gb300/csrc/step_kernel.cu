@@ -42,12 +42,15 @@ __host__ __device__ constexpr int hDn(int j) { return (int)((kDnBits >> (5 * j))
 
 template <int TY>
 struct Geo {
-    static constexpr int NTH = TILE_X * TY;
+    static constexpr int NOWN = TILE_X * TY;    // owner threads: one per column, one warp per row
+    static constexpr int NR = 2 * TILE_X + 2 * TY + 4;  // rim columns
+    static constexpr int NRW = (NR + 31) / 32;  // dedicated rim warps
+    static constexpr int NTH = NOWN + 32 * NRW;
     static constexpr int W = TILE_X + 2;        // shared-memory row pitch (column + rim)
     static constexpr int NCOL = W * (TY + 2);   // columns incl. rim
-    static constexpr int NR = 2 * TILE_X + 2 * TY + 4;
     static constexpr int PLANE = 8 * NCOL;      // floats of one 8-population plane buffer
     static constexpr int SMEM = 6 * PLANE * 4;  // up x3, flat x2, down x1
+    static constexpr int MINB = TY == 4 ? 4 : (TY == 8 ? 2 : 1);  // resident CTAs per SM targeted
 };
 
 constexpr bool need_dir(int q, int rcx, int rcy) {
@@ -268,8 +271,10 @@ __device__ __forceinline__ void arrive_rim(const float raw[10], float rho0, cons
 }
 
 // SPECIAL = false: every node of every item is a plain bulk node (no node words are read).
+// Threads [0, NOWN) own one column each (a warp per row) and emit it; the NRW rim warps only
+// rebuild the one-node rim, so both kinds finish a plane's arrive phase at about the same time.
 template <typename S, int TY, bool SPECIAL>
-__global__ void __launch_bounds__(TILE_X *TY, (TY == 4 ? 5 : (TY == 8 ? 3 : 1)))
+__global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     step_kernel(const StepArgs *__restrict__ ga, const int parity, double *__restrict__ force,
                 double *__restrict__ diag_part) {
     using G = Geo<TY>;
@@ -285,6 +290,7 @@ __global__ void __launch_bounds__(TILE_X *TY, (TY == 4 ? 5 : (TY == 8 ? 3 : 1)))
     const float omega = ga->omega, rho0 = ga->rho0;
     const StorageScale sc = ga->sc;
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const bool owner = tid < G::NOWN;
     const int64_t plane = (int64_t)nx * ny;
     const bool diag = diag_part != nullptr;
     double dmD = 0.0, deD = 0.0;
@@ -297,33 +303,37 @@ __global__ void __launch_bounds__(TILE_X *TY, (TY == 4 ? 5 : (TY == 8 ? 3 : 1)))
         const int w = min(TILE_X, nx - x0), h = min(TY, ny - y0);
         const int zs = seg * lz, ze = min(zs + lz, nz);
         const int slot = (SPECIAL && tile_slot) ? tile_slot[tile] : -1;
-        const bool own = tx < w && ty < h;
+        const bool own = owner && tx < w && ty < h;
         const int x = x0 + tx, y = y0 + ty;
         const int col = (ty + 1) * G::W + (tx + 1);
-        const int64_t xy = own ? (int64_t)x + (int64_t)nx * y : 0;
-
-        // rim column of this thread (if any)
-        int rside = -1, rcol = 0;
-        int64_t rxy = 0;
-        if (tid < G::NR) {
+        // the column this thread loads and rebuilds: its own, or a rim column for rim warps
+        int rside = -1, ccol = col;
+        int64_t cxy = 0;
+        bool active = own;
+        if (own) {
+            cxy = (int64_t)x + (int64_t)nx * y;
+        } else if (!owner) {
             int rx, ry, sd;
-            const int r = tid;
+            const int r = tid - G::NOWN;
             if (r < TILE_X) { rx = r; ry = -1; sd = 0; }
             else if (r < 2 * TILE_X) { rx = r - TILE_X; ry = h; sd = 1; }
             else if (r < 2 * TILE_X + TY) { rx = -1; ry = r - 2 * TILE_X; sd = 2; }
             else if (r < 2 * TILE_X + 2 * TY) { rx = w; ry = r - 2 * TILE_X - TY; sd = 3; }
-            else {
+            else if (r < G::NR) {
                 const int k = r - 2 * TILE_X - 2 * TY;
                 rx = (k & 1) ? w : -1;
                 ry = (k & 2) ? h : -1;
                 sd = 4 + k;
-            }
-            const bool valid = (sd == 0 || sd == 1) ? rx < w : ((sd == 2 || sd == 3) ? ry < h : true);
+            } else { rx = 0; ry = 0; sd = -1; }
+            const bool valid = sd >= 0 && ((sd == 0 || sd == 1) ? rx < w : ((sd == 2 || sd == 3) ? ry < h : true));
             if (valid) {
                 rside = sd;
-                rcol = (ry + 1) * G::W + (rx + 1);
-                const int gx = (x0 + rx + nx) % nx, gy = (y0 + ry + ny) % ny;
-                rxy = (int64_t)gx + (int64_t)nx * gy;
+                ccol = (ry + 1) * G::W + (rx + 1);
+                int gx = x0 + rx, gy = y0 + ry;
+                gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
+                gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
+                cxy = (int64_t)gx + (int64_t)nx * gy;
+                active = true;
             }
         }
 
@@ -331,38 +341,39 @@ __global__ void __launch_bounds__(TILE_X *TY, (TY == 4 ? 5 : (TY == 8 ? 3 : 1)))
         float c0 = 0.f, c5 = 0.f, c6 = 0.f;  // own-column rest / up / down populations of the newest plane
         float p0 = 0.f, p5 = 0.f, pp5 = 0.f; // history: f0(z), f5(z), f5(z-1)
         float dm = 0.f, de = 0.f;
-        const int zm = (zs - 1 + nz) % nz;
-        if (own) load_raw<S>(src, fs, xy + (int64_t)zm * plane, pre);
+        const int zm = zs == 0 ? nz - 1 : zs - 1;
+        if (active) load_raw<S>(src, fs, cxy + (int64_t)zm * plane, pre);
+        int zn = zs;  // plane of the next prefetch (wrapped)
 
         // prologue: planes zs-1 (ring slot 0) and zs (slot 1); then march
         for (int k = 0; k <= ze - zs + 1; ++k) {
-            const int p = zs - 1 + k;  // plane arriving in ring slot k
             float *up = smem + (k % 3) * G::PLANE;
             float *flt = smem + (3 + (k & 1)) * G::PLANE;
             float *dn = smem + 5 * G::PLANE;
-            float rv[10];
-            if (rside >= 0) load_raw<S>(src, fs, rxy + (int64_t)((p + nz) % nz) * plane, rv);
-            if (own) {
+            if (active) {
                 float cur[10];
 #pragma unroll
                 for (int i = 0; i < 10; ++i) cur[i] = pre[i];
-                if (p + 1 <= ze) load_raw<S>(src, fs, xy + (int64_t)((p + 1) % nz) * plane, pre);
-                arrive_own<S, TY>(cur, rho0, sc, up, flt, dn, col, c0, c5, c6);
+                if (zs + k <= ze) {
+                    load_raw<S>(src, fs, cxy + (int64_t)zn * plane, pre);
+                    zn = zn + 1 == nz ? 0 : zn + 1;
+                }
+                if (owner) arrive_own<S, TY>(cur, rho0, sc, up, flt, dn, col, c0, c5, c6);
+                else arrive_rim<S, TY>(cur, rho0, sc, rside, up, flt, dn, ccol);
             }
-            if (rside >= 0) arrive_rim<S, TY>(rv, rho0, sc, rside, up, flt, dn, rcol);
             if (k < 2) {
                 pp5 = p5;
                 p5 = c5;
                 p0 = c0;
                 continue;
             }
-            // emit plane z = p - 1 (its down populations come from plane p, just written)
-            const int z = p - 1;
+            // emit plane z (its down populations come from plane z+1, just written)
+            const int z = zs + k - 2;
             __syncthreads();
             if (own) {
                 const float *eup = smem + ((k - 2) % 3) * G::PLANE;  // plane z-1
                 const float *efl = smem + (3 + ((k - 1) & 1)) * G::PLANE;  // plane z
-                const int64_t node = xy + (int64_t)z * plane;
+                const int64_t node = cxy + (int64_t)z * plane;
                 const uint32_t wd = (SPECIAL && slot >= 0) ? word[node] : 0u;
                 if (wd == 0u) {
                     Mom m;
@@ -398,13 +409,13 @@ __global__ void __launch_bounds__(TILE_X *TY, (TY == 4 ? 5 : (TY == 8 ? 3 : 1)))
     }
 
     if (diag) {
-        // deterministic block reduction of the FP64 partials -> diag_part[blockIdx.x]
+        // deterministic block reduction of the owner threads' FP64 partials -> diag_part[blockIdx.x]
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             dmD += __shfl_down_sync(0xffffffffu, dmD, o);
             deD += __shfl_down_sync(0xffffffffu, deD, o);
         }
-        if (tx == 0) {
+        if (tx == 0 && owner) {
             red[0][ty] = dmD;
             red[1][ty] = deD;
         }
