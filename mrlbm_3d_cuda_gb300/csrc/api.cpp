@@ -142,8 +142,8 @@ int ensure_stage(mrlbm_handle *h, size_t bytes) {
 int choose_tiling(mrlbm_handle *h) {
     const char *ety = std::getenv("MRLBM_TILE_Y");
     const char *elz = std::getenv("MRLBM_LZ");
-    int ty = ety ? std::atoi(ety) : 8;
-    if (ty != 4 && ty != 8 && ty != 16) ty = 8;
+    int ty = ety ? std::atoi(ety) : 4;
+    if (ty != 4 && ty != 8 && ty != 16) ty = 4;
     h->tile_y = ty;
     h->tiles_x = (h->d.nx + TILE_X - 1) / TILE_X;
     h->tiles_y = (h->d.ny + ty - 1) / ty;
@@ -304,7 +304,7 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     }
     const Geometry &g = h->geo;
     h->n = (int64_t)d.nx * d.ny * d.nz;
-    h->fs = (h->n + 63) / 64 * 64;  // 256-byte aligned field planes for any storage type
+    h->fs = aos_elements(d.nx, d.ny, d.nz);  // storage elements per moment buffer
     h->storage = d.storage;
     h->vbytes = d.storage == MRLBM_STORAGE_F32 ? 4 : 2;
     for (int k = 0; k < 3; ++k) {
@@ -357,7 +357,7 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     h->n_ctas = std::max(1, std::min(h->n_items, resident));
 
     mrlbm_handle *H = h.get();
-    const size_t mbytes = (size_t)h->fs * 10 * h->vbytes;
+    const size_t mbytes = (size_t)h->fs * h->vbytes;
     CK(H, cudaMalloc(&h->m[0], mbytes));
     CK(H, cudaMalloc(&h->m[1], mbytes));
     CK(H, cudaMemset(h->m[0], 0, mbytes));
@@ -399,7 +399,7 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     StepArgs &a = h->args;
     a.m[0] = h->m[0];
     a.m[1] = h->m[1];
-    a.fs = h->fs;
+    a.nxb = (d.nx + kXBlock - 1) / kXBlock;
     a.word = h->d_word;
     a.items = h->d_items;
     a.n_items = h->n_items;
@@ -495,7 +495,6 @@ int mrlbm_init(mrlbm_handle *h, int32_t kind, const double *params, int32_t n_pa
     InitArgs ia;
     ia.m_a = h->m[0];
     ia.m_b = h->m[1];
-    ia.fs = h->fs;
     ia.nx = h->d.nx;
     ia.ny = h->d.ny;
     ia.nz = h->d.nz;
@@ -589,21 +588,11 @@ int mrlbm_get_moments(mrlbm_handle *h, uint32_t mask, int32_t layout, float *hos
     if (layout != MRLBM_LAYOUT_LEXICOGRAPHIC && layout != MRLBM_LAYOUT_REF_TILED)
         return fail(h, MRLBM_ERR_INVALID_ARG, "bad layout");
     const void *src = h->m[h->parity];
-    if (h->storage == MRLBM_STORAGE_F32 && layout == MRLBM_LAYOUT_LEXICOGRAPHIC) {
-        int k = 0;
-        for (int f = 0; f < 10; ++f) {
-            if (!(mask & (1u << f))) continue;
-            CK(h, cudaMemcpyAsync(host + (size_t)k * h->n, (const float *)src + (size_t)f * h->fs, h->n * 4,
-                                  cudaMemcpyDeviceToHost, h->stream));
-            ++k;
-        }
-    } else {
-        int rc = ensure_stage(h, (size_t)nf * h->n * 4);
-        if (rc) return rc;
-        CK(h, launch_convert(src, nullptr, nullptr, h->d_stage, h->fs, mask, layout, h->d.nx, h->d.ny, h->d.nz,
-                             h->storage, h->sc, 0, h->stream));
-        CK(h, cudaMemcpyAsync(host, h->d_stage, (size_t)nf * h->n * 4, cudaMemcpyDeviceToHost, h->stream));
-    }
+    int rc = ensure_stage(h, (size_t)nf * h->n * 4);
+    if (rc) return rc;
+    CK(h, launch_convert(src, nullptr, nullptr, h->d_stage, mask, layout, h->d.nx, h->d.ny, h->d.nz, h->storage, h->sc,
+                         0, h->stream));
+    CK(h, cudaMemcpyAsync(host, h->d_stage, (size_t)nf * h->n * 4, cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     return MRLBM_OK;
 }
@@ -619,22 +608,11 @@ int mrlbm_set_moments(mrlbm_handle *h, uint32_t mask, int32_t layout, const floa
     if (layout != MRLBM_LAYOUT_LEXICOGRAPHIC && layout != MRLBM_LAYOUT_REF_TILED)
         return fail(h, MRLBM_ERR_INVALID_ARG, "bad layout");
     void *cur = h->m[h->parity], *oth = h->m[h->parity ^ 1];
-    if (h->storage == MRLBM_STORAGE_F32 && layout == MRLBM_LAYOUT_LEXICOGRAPHIC) {
-        int k = 0;
-        for (int f = 0; f < 10; ++f) {
-            if (!(mask & (1u << f))) continue;
-            float *dc = (float *)cur + (size_t)f * h->fs, *dn = (float *)oth + (size_t)f * h->fs;
-            CK(h, cudaMemcpyAsync(dc, host + (size_t)k * h->n, h->n * 4, cudaMemcpyHostToDevice, h->stream));
-            CK(h, cudaMemcpyAsync(dn, dc, h->n * 4, cudaMemcpyDeviceToDevice, h->stream));
-            ++k;
-        }
-    } else {
-        int rc = ensure_stage(h, (size_t)nf * h->n * 4);
-        if (rc) return rc;
-        CK(h, cudaMemcpyAsync(h->d_stage, host, (size_t)nf * h->n * 4, cudaMemcpyHostToDevice, h->stream));
-        CK(h, launch_convert(nullptr, cur, oth, h->d_stage, h->fs, mask, layout, h->d.nx, h->d.ny, h->d.nz, h->storage,
-                             h->sc, 1, h->stream));
-    }
+    int rc = ensure_stage(h, (size_t)nf * h->n * 4);
+    if (rc) return rc;
+    CK(h, cudaMemcpyAsync(h->d_stage, host, (size_t)nf * h->n * 4, cudaMemcpyHostToDevice, h->stream));
+    CK(h, launch_convert(nullptr, cur, oth, h->d_stage, mask, layout, h->d.nx, h->d.ny, h->d.nz, h->storage, h->sc, 1,
+                         h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     h->initialized = true;
     return MRLBM_OK;

@@ -7,6 +7,15 @@
 
 namespace mrlbm {
 
+// x-blocked, field-interleaved moment layout (see storage.cuh).
+constexpr int kXBlock = 32;
+inline __host__ __device__ int64_t aos_index(int x, int y, int z, int nxb, int ny) {
+    return ((((int64_t)z * ny + y) * nxb + (x >> 5)) * 10) * kXBlock + (x & (kXBlock - 1));
+}
+inline __host__ __device__ int64_t aos_elements(int nx, int ny, int nz) {
+    return (int64_t)nz * ny * ((nx + kXBlock - 1) / kXBlock) * 10 * kXBlock;
+}
+
 // Low-precision storage keeps scaled deviations from the rest state: stored = value * scale,
 // one scale for rho - rho0, one for u, one for m.
 struct StorageScale {
@@ -28,8 +37,8 @@ struct WallArgs {
 // One copy lives in device memory per handle; kernels receive a pointer to it plus the
 // per-step scalars (ping-pong parity, sampling buffers).
 struct StepArgs {
-    void *m[2] = {nullptr, nullptr};  // ping-pong moment buffers, 10 fields, field stride `fs`
-    int64_t fs = 0;
+    void *m[2] = {nullptr, nullptr};  // ping-pong moment buffers (aos layout)
+    int nxb = 0;                      // 32-node x-blocks per row
     const uint32_t *word = nullptr;     // internal node words (lexicographic); null if all bulk
     const int32_t *items = nullptr;     // work items: tile index | (z-segment << 20)
     int n_items = 0;
@@ -72,7 +81,6 @@ cudaError_t launch_diag_finalize(const double *part, int n, double *out, cudaStr
 
 struct InitArgs {
     void *m_a = nullptr, *m_b = nullptr;  // both ping-pong buffers
-    int64_t fs = 0;
     int nx = 0, ny = 0, nz = 0;
     int kind = 0;
     double p[8] = {0};
@@ -83,7 +91,7 @@ cudaError_t launch_init(const InitArgs &a, int storage, cudaStream_t s);
 
 // Convert between device storage and an FP32 staging buffer (lexicographic or reference
 // tiled layout).  dir = 0: storage -> f32, 1: f32 -> storage (written to dst_a and dst_b).
-cudaError_t launch_convert(const void *src, void *dst_a, void *dst_b, float *f32, int64_t fs, uint32_t field_mask,
+cudaError_t launch_convert(const void *src, void *dst_a, void *dst_b, float *f32, uint32_t field_mask,
                            int layout, int nx, int ny, int nz, int storage, const StorageScale &sc, int dir,
                            cudaStream_t s);
 

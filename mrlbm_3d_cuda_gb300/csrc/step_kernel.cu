@@ -89,7 +89,7 @@ __device__ __noinline__ int special_node(const StepArgs *__restrict__ ga, int pa
     if (cls == C_BULK) {
         evaluate(fl, m);
     } else {
-        const Mom prev = load_mom<S>(src, a.fs, node, a.rho0, a.sc);
+        const Mom prev = load_mom<S>(src, aos_index(x, y, z, a.nxb, a.ny), a.rho0, a.sc);
         m = prev;  // nodes without a closure keep their pre-stream moments
         if (cls == C_SOLID) {
             fluid = false;
@@ -110,7 +110,7 @@ __device__ __noinline__ int special_node(const StepArgs *__restrict__ ga, int pa
             c.rho0 = a.rho0;
             c.convective = a.convective;
             c.self_prev = prev;
-            if (class_walls(cls) & 2u) c.west_prev = load_mom<S>(src, a.fs, node - 1, a.rho0, a.sc);
+            if (class_walls(cls) & 2u) c.west_prev = load_mom<S>(src, aos_index(x - 1, y, z, a.nxb, a.ny), a.rho0, a.sc);
             else c.west_prev = prev;
             Mom o = prev;
             if (planar_closure(cls, fl, c, o)) m = o;
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     __shared__ double red[2][TY];
     const S *__restrict__ src = (const S *)ga->m[parity];
     S *__restrict__ dst = (S *)ga->m[parity ^ 1];
-    const int64_t fs = ga->fs;
+    const int nxb = ga->nxb;
     const int nx = ga->nx, ny = ga->ny, nz = ga->nz, lz = ga->lz, tiles_x = ga->tiles_x, n_items = ga->n_items;
     const int32_t *__restrict__ items = ga->items;
     const int32_t *__restrict__ tile_slot = ga->tile_slot;
@@ -291,7 +291,8 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     const StorageScale sc = ga->sc;
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
     const bool owner = tid < G::NOWN;
-    const int64_t plane = (int64_t)nx * ny;
+    const int64_t plane = (int64_t)nx * ny;                 // lexicographic plane (node words)
+    const int64_t zst = (int64_t)ny * nxb * 10 * kXBlock;  // storage elements per z plane
     const bool diag = diag_part != nullptr;
     double dmD = 0.0, deD = 0.0;
 
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         int64_t cxy = 0;
         bool active = own;
         if (own) {
-            cxy = (int64_t)x + (int64_t)nx * y;
+            cxy = aos_index(x, y, 0, nxb, ny);
         } else if (!owner) {
             int rx, ry, sd;
             const int r = tid - G::NOWN;
@@ -332,7 +333,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 int gx = x0 + rx, gy = y0 + ry;
                 gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
                 gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
-                cxy = (int64_t)gx + (int64_t)nx * gy;
+                cxy = aos_index(gx, gy, 0, nxb, ny);
                 active = true;
             }
         }
@@ -342,7 +343,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         float p0 = 0.f, p5 = 0.f, pp5 = 0.f; // history: f0(z), f5(z), f5(z-1)
         float dm = 0.f, de = 0.f;
         const int zm = zs == 0 ? nz - 1 : zs - 1;
-        if (active) load_raw<S>(src, fs, cxy + (int64_t)zm * plane, pre);
+        if (active) load_raw<S>(src, cxy + (int64_t)zm * zst, pre);
         int zn = zs;  // plane of the next prefetch (wrapped)
 
         // prologue: planes zs-1 (ring slot 0) and zs (slot 1); then march
@@ -355,7 +356,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
 #pragma unroll
                 for (int i = 0; i < 10; ++i) cur[i] = pre[i];
                 if (zs + k <= ze) {
-                    load_raw<S>(src, fs, cxy + (int64_t)zn * plane, pre);
+                    load_raw<S>(src, cxy + (int64_t)zn * zst, pre);
                     zn = zn + 1 == nz ? 0 : zn + 1;
                 }
                 if (owner) arrive_own<S, TY>(cur, rho0, sc, up, flt, dn, col, c0, c5, c6);
@@ -373,7 +374,8 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
             if (own) {
                 const float *eup = smem + ((k - 2) % 3) * G::PLANE;  // plane z-1
                 const float *efl = smem + (3 + ((k - 1) & 1)) * G::PLANE;  // plane z
-                const int64_t node = cxy + (int64_t)z * plane;
+                const int64_t ai = cxy + (int64_t)z * zst;
+                const int64_t node = (int64_t)x + (int64_t)nx * y + (int64_t)z * plane;
                 const uint32_t wd = (SPECIAL && slot >= 0) ? word[node] : 0u;
                 if (wd == 0u) {
                     Mom m;
@@ -383,14 +385,14 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                         de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
                     }
                     collide(m, omega);
-                    store_mom<S>(dst, fs, node, m, rho0, sc);
+                    store_mom<S>(dst, ai, m, rho0, sc);
                 } else if constexpr (SPECIAL) {
                     float fw[27];
                     gather_all<TY>(eup, efl, dn, col, p0, pp5, c6, fw);
                     Mom ms;
                     const int code =
                         special_node<S, TY>(ga, parity, force != nullptr, wd, fw, x, y, z, node, slot, x0, y0, ms);
-                    if (code) store_mom<S>(dst, fs, node, ms, rho0, sc);
+                    if (code) store_mom<S>(dst, ai, ms, rho0, sc);
                     if (code == 2 && diag) {
                         dm += ms.rho - rho0;
                         de += 0.5f * (ms.ux * ms.ux + ms.uy * ms.uy + ms.uz * ms.uz);

@@ -1,6 +1,8 @@
-// Moment storage in HBM: 10 field-major planes (rho - rho0, ux, uy, uz, mxx, myy, mzz, mxy,
-// mxz, myz), each `fs` elements, lexicographic node order.  FP32, or FP16 / BF16 holding
-// scaled deviations from the rest state (rho0, u = 0, m = 0).
+// Moment storage in HBM, x-blocked and field-interleaved: the 32 nodes x = 32 b .. 32 b + 31 of
+// one (y, z) row keep their 10 fields (rho - rho0, ux, uy, uz, mxx, myy, mzz, mxy, mxz, myz)
+// in one contiguous run of 10 x 32 values, so a warp reads or writes a field of its row as
+// one 128-byte line and all 10 fields of a node sit at constant offsets from one address.
+// FP32, or FP16 / BF16 holding scaled deviations from the rest state (rho0, u = 0, m = 0).
 #pragma once
 
 #include <cuda_bf16.h>
@@ -51,45 +53,47 @@ __device__ __forceinline__ Mom decode(const float v[10], float rho0, const Stora
     return m;
 }
 
+// `ai` is the element index of field 0 of a node (aos_index); field k sits at ai + 32 k.
 template <typename S>
-__device__ __forceinline__ void load_raw(const S *__restrict__ base, int64_t fs, int64_t node, float v[10]) {
+__device__ __forceinline__ void load_raw(const S *__restrict__ base, int64_t ai, float v[10]) {
+    const S *p = base + ai;
 #pragma unroll
-    for (int k = 0; k < 10; ++k) v[k] = to_f<S>(base[k * fs + node]);
+    for (int k = 0; k < 10; ++k) v[k] = to_f<S>(p[k * kXBlock]);
 }
 
 template <typename S>
-__device__ __forceinline__ Mom load_mom(const S *__restrict__ base, int64_t fs, int64_t node, float rho0,
-                                        const StorageScale &sc) {
+__device__ __forceinline__ Mom load_mom(const S *__restrict__ base, int64_t ai, float rho0, const StorageScale &sc) {
     float v[10];
-    load_raw<S>(base, fs, node, v);
+    load_raw<S>(base, ai, v);
     return decode<S>(v, rho0, sc);
 }
 
 template <typename S>
-__device__ __forceinline__ void store_mom(S *__restrict__ base, int64_t fs, int64_t node, const Mom &m, float rho0,
+__device__ __forceinline__ void store_mom(S *__restrict__ base, int64_t ai, const Mom &m, float rho0,
                                           const StorageScale &sc) {
+    S *p = base + ai;
     if constexpr (std::is_same<S, float>::value) {
-        base[0 * fs + node] = m.rho - rho0;
-        base[1 * fs + node] = m.ux;
-        base[2 * fs + node] = m.uy;
-        base[3 * fs + node] = m.uz;
-        base[4 * fs + node] = m.mxx;
-        base[5 * fs + node] = m.myy;
-        base[6 * fs + node] = m.mzz;
-        base[7 * fs + node] = m.mxy;
-        base[8 * fs + node] = m.mxz;
-        base[9 * fs + node] = m.myz;
+        p[0 * kXBlock] = m.rho - rho0;
+        p[1 * kXBlock] = m.ux;
+        p[2 * kXBlock] = m.uy;
+        p[3 * kXBlock] = m.uz;
+        p[4 * kXBlock] = m.mxx;
+        p[5 * kXBlock] = m.myy;
+        p[6 * kXBlock] = m.mzz;
+        p[7 * kXBlock] = m.mxy;
+        p[8 * kXBlock] = m.mxz;
+        p[9 * kXBlock] = m.myz;
     } else {
-        base[0 * fs + node] = from_f<S>((m.rho - rho0) * sc.s[0]);
-        base[1 * fs + node] = from_f<S>(m.ux * sc.s[1]);
-        base[2 * fs + node] = from_f<S>(m.uy * sc.s[1]);
-        base[3 * fs + node] = from_f<S>(m.uz * sc.s[1]);
-        base[4 * fs + node] = from_f<S>(m.mxx * sc.s[2]);
-        base[5 * fs + node] = from_f<S>(m.myy * sc.s[2]);
-        base[6 * fs + node] = from_f<S>(m.mzz * sc.s[2]);
-        base[7 * fs + node] = from_f<S>(m.mxy * sc.s[2]);
-        base[8 * fs + node] = from_f<S>(m.mxz * sc.s[2]);
-        base[9 * fs + node] = from_f<S>(m.myz * sc.s[2]);
+        p[0 * kXBlock] = from_f<S>((m.rho - rho0) * sc.s[0]);
+        p[1 * kXBlock] = from_f<S>(m.ux * sc.s[1]);
+        p[2 * kXBlock] = from_f<S>(m.uy * sc.s[1]);
+        p[3 * kXBlock] = from_f<S>(m.uz * sc.s[1]);
+        p[4 * kXBlock] = from_f<S>(m.mxx * sc.s[2]);
+        p[5 * kXBlock] = from_f<S>(m.myy * sc.s[2]);
+        p[6 * kXBlock] = from_f<S>(m.mzz * sc.s[2]);
+        p[7 * kXBlock] = from_f<S>(m.mxy * sc.s[2]);
+        p[8 * kXBlock] = from_f<S>(m.mxz * sc.s[2]);
+        p[9 * kXBlock] = from_f<S>(m.myz * sc.s[2]);
     }
 }
 

@@ -81,31 +81,33 @@ __global__ void init_kernel(const InitArgs a) {
         }
         default: break;
     }
-    store_mom<S>((S *)a.m_a, a.fs, i, m, a.rho0, a.sc);
-    store_mom<S>((S *)a.m_b, a.fs, i, m, a.rho0, a.sc);
+    const int64_t ai = aos_index(x, y, z, (a.nx + kXBlock - 1) / kXBlock, a.ny);
+    store_mom<S>((S *)a.m_a, ai, m, a.rho0, a.sc);
+    store_mom<S>((S *)a.m_b, ai, m, a.rho0, a.sc);
 }
 
 template <typename S>
-__global__ void convert_kernel(const S *src, S *dst_a, S *dst_b, float *f32, int64_t fs, uint32_t mask, int layout,
+__global__ void convert_kernel(const S *src, S *dst_a, S *dst_b, float *f32, uint32_t mask, int layout,
                                int nx, int ny, int nz, StorageScale sc, int dir) {
     const int64_t n = (int64_t)nx * ny * nz;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((int64_t)nx * ny));
     const int64_t h = layout == MRLBM_LAYOUT_REF_TILED ? ref_tiled_index(x, y, z, nx, ny) : i;
+    const int64_t ai = aos_index(x, y, z, (nx + kXBlock - 1) / kXBlock, ny);
     int slot = 0;
     for (int f = 0; f < 10; ++f) {
         if (!(mask & (1u << f))) continue;
         const float s = sc.s[scale_class(f)], is = sc.is[scale_class(f)];
         const bool lowp = !std::is_same<S, float>::value;
         if (dir == 0) {
-            const float v = to_f<S>(src[f * fs + i]);
+            const float v = to_f<S>(src[ai + f * kXBlock]);
             f32[(int64_t)slot * n + h] = lowp ? v * is : v;
         } else {
             const float v = f32[(int64_t)slot * n + h];
             const S sv = from_f<S>(lowp ? v * s : v);
-            dst_a[f * fs + i] = sv;
-            if (dst_b) dst_b[f * fs + i] = sv;
+            dst_a[ai + f * kXBlock] = sv;
+            if (dst_b) dst_b[ai + f * kXBlock] = sv;
         }
         ++slot;
     }
@@ -125,23 +127,23 @@ cudaError_t launch_init(const InitArgs &a, int storage, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_convert(const void *src, void *dst_a, void *dst_b, float *f32, int64_t fs, uint32_t field_mask,
+cudaError_t launch_convert(const void *src, void *dst_a, void *dst_b, float *f32, uint32_t field_mask,
                            int layout, int nx, int ny, int nz, int storage, const StorageScale &sc, int dir,
                            cudaStream_t s) {
     const int64_t n = (int64_t)nx * ny * nz;
     const unsigned blocks = (unsigned)((n + 255) / 256);
     switch (storage) {
         case MRLBM_STORAGE_F32:
-            convert_kernel<float><<<blocks, 256, 0, s>>>((const float *)src, (float *)dst_a, (float *)dst_b, f32, fs,
+            convert_kernel<float><<<blocks, 256, 0, s>>>((const float *)src, (float *)dst_a, (float *)dst_b, f32,
                                                          field_mask, layout, nx, ny, nz, sc, dir);
             break;
         case MRLBM_STORAGE_F16:
-            convert_kernel<__half><<<blocks, 256, 0, s>>>((const __half *)src, (__half *)dst_a, (__half *)dst_b, f32, fs,
+            convert_kernel<__half><<<blocks, 256, 0, s>>>((const __half *)src, (__half *)dst_a, (__half *)dst_b, f32,
                                                           field_mask, layout, nx, ny, nz, sc, dir);
             break;
         case MRLBM_STORAGE_BF16:
             convert_kernel<__nv_bfloat16><<<blocks, 256, 0, s>>>((const __nv_bfloat16 *)src, (__nv_bfloat16 *)dst_a,
-                                                                 (__nv_bfloat16 *)dst_b, f32, fs, field_mask, layout,
+                                                                 (__nv_bfloat16 *)dst_b, f32, field_mask, layout,
                                                                  nx, ny, nz, sc, dir);
             break;
         default: return cudaErrorInvalidValue;
