@@ -49,8 +49,9 @@ struct Geo {
     static constexpr int W = TILE_X + 2;        // shared-memory row pitch (column + rim)
     static constexpr int NCOL = W * (TY + 2);   // columns incl. rim
     static constexpr int PLANE = 8 * NCOL;      // floats of one 8-population plane buffer
-    static constexpr int SMEM = 6 * PLANE * 4;  // up x3, flat x2, down x1
-    static constexpr int MINB = TY == 4 ? 4 : (TY == 8 ? 2 : 1);  // resident CTAs per SM targeted
+    static constexpr int NUP = 4, NFL = 3, NDN = 2;  // ring depths (rim warps run one plane ahead)
+    static constexpr int SMEM = (NUP + NFL + NDN) * PLANE * 4;
+    static constexpr int MINB = TY == 4 ? 3 : (TY == 8 ? 2 : 1);  // resident CTAs per SM targeted
 };
 
 constexpr bool need_dir(int q, int rcx, int rcy) {
@@ -270,9 +271,27 @@ __device__ __forceinline__ void arrive_rim(const float raw[10], float rho0, cons
     }
 }
 
+// Named CTA barriers (PTX bar.sync / bar.arrive; id 0 is __syncthreads).  A generation
+// completes when `n` threads (whole warps) have arrived; bar.arrive does not wait.
+__device__ __forceinline__ void nb_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void nb_arrive(int id, int n) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
 // SPECIAL = false: every node of every item is a plain bulk node (no node words are read).
-// Threads [0, NOWN) own one column each (a warp per row) and emit it; the NRW rim warps only
-// rebuild the one-node rim, so both kinds finish a plane's arrive phase at about the same time.
+//
+// Warp roles and schedule per work item (planes indexed k = 0 .. L+1 from zs-1, L = ze-zs):
+//   owner warps (one per tile row):  rebuild own columns of plane k; for k >= 2 wait FULL(k),
+//       emit plane k-1 (reads up(k-2), flat(k-1), down(k)), then signal DONE(k) if a rim
+//       iteration k+2 will wait for it;
+//   rim warps:  for k >= 4 wait DONE(k-2); rebuild the rim columns of plane k; for k >= 2
+//       signal FULL(k).
+// Plane k's buffers live in ring slots up[k%4], flat[k%3], down[k%2]; their previous
+// occupants (plane k-4 / k-3 / k-2) are last read by the emit of iteration k-2, which both
+// roles wait for before writing (owners through FULL(k-1)).  FULL(k) / DONE(k) use barrier ids
+// 1 + (k&1) / 3 + (k&1); a role can run at most one generation ahead on an id, so
+// consecutive generations never mix.  Counts are always the whole CTA (owner arrivals +
+// rim arrivals), so the rim work of the next plane overlaps the owners' emit.
 template <typename S, int TY, bool SPECIAL>
 __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     step_kernel(const StepArgs *__restrict__ ga, const int parity, double *__restrict__ force,
@@ -294,6 +313,9 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     const int64_t plane = (int64_t)nx * ny;                 // lexicographic plane (node words)
     const int64_t zst = (int64_t)ny * nxb * 10 * kXBlock;  // storage elements per z plane
     const bool diag = diag_part != nullptr;
+    float *const up_base = smem;
+    float *const fl_base = smem + G::NUP * G::PLANE;
+    float *const dn_base = smem + (G::NUP + G::NFL) * G::PLANE;
     double dmD = 0.0, deD = 0.0;
 
     for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
@@ -303,6 +325,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         const int x0 = tix * TILE_X, y0 = tiy * TY;
         const int w = min(TILE_X, nx - x0), h = min(TY, ny - y0);
         const int zs = seg * lz, ze = min(zs + lz, nz);
+        const int last = ze - zs + 1;  // last plane index k
         const int slot = (SPECIAL && tile_slot) ? tile_slot[tile] : -1;
         const bool own = owner && tx < w && ty < h;
         const int x = x0 + tx, y = y0 + ty;
@@ -339,75 +362,92 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         }
 
         float pre[10];
-        float c0 = 0.f, c5 = 0.f, c6 = 0.f;  // own-column rest / up / down populations of the newest plane
-        float p0 = 0.f, p5 = 0.f, pp5 = 0.f; // history: f0(z), f5(z), f5(z-1)
-        float dm = 0.f, de = 0.f;
         const int zm = zs == 0 ? nz - 1 : zs - 1;
         if (active) load_raw<S>(src, cxy + (int64_t)zm * zst, pre);
         int zn = zs;  // plane of the next prefetch (wrapped)
+        int k3 = 0, k4 = 0;  // k % 3, k % 4
 
-        // prologue: planes zs-1 (ring slot 0) and zs (slot 1); then march
-        for (int k = 0; k <= ze - zs + 1; ++k) {
-            float *up = smem + (k % 3) * G::PLANE;
-            float *flt = smem + (3 + (k & 1)) * G::PLANE;
-            float *dn = smem + 5 * G::PLANE;
-            if (active) {
-                float cur[10];
+        if (owner) {
+            float c0 = 0.f, c5 = 0.f, c6 = 0.f;   // own-column rest / up / down populations of plane k
+            float p0 = 0.f, p5 = 0.f, pp5 = 0.f;  // f0(k-1), f5(k-1), f5(k-2)
+            float dm = 0.f, de = 0.f;
+            for (int k = 0; k <= last; ++k) {
+                float *up = up_base + k4 * G::PLANE;
+                float *flt = fl_base + k3 * G::PLANE;
+                float *dn = dn_base + (k & 1) * G::PLANE;
+                if (own) {
+                    float cur[10];
 #pragma unroll
-                for (int i = 0; i < 10; ++i) cur[i] = pre[i];
-                if (zs + k <= ze) {
-                    load_raw<S>(src, cxy + (int64_t)zn * zst, pre);
-                    zn = zn + 1 == nz ? 0 : zn + 1;
+                    for (int i = 0; i < 10; ++i) cur[i] = pre[i];
+                    if (k < last) {
+                        load_raw<S>(src, cxy + (int64_t)zn * zst, pre);
+                        zn = zn + 1 == nz ? 0 : zn + 1;
+                    }
+                    arrive_own<S, TY>(cur, rho0, sc, up, flt, dn, col, c0, c5, c6);
                 }
-                if (owner) arrive_own<S, TY>(cur, rho0, sc, up, flt, dn, col, c0, c5, c6);
-                else arrive_rim<S, TY>(cur, rho0, sc, rside, up, flt, dn, ccol);
-            }
-            if (k < 2) {
+                if (k >= 2) {
+                    nb_sync(1 + (k & 1), G::NTH);  // FULL(k): plane k complete, emits of k-1 done
+                    const int z = zs + k - 2;      // emitted plane
+                    if (own) {
+                        const float *eup = up_base + (k4 >= 2 ? k4 - 2 : k4 + 2) * G::PLANE;  // plane k-2
+                        const float *efl = fl_base + (k3 >= 1 ? k3 - 1 : 2) * G::PLANE;       // plane k-1
+                        const int64_t ai = cxy + (int64_t)z * zst;
+                        const int64_t node = (int64_t)x + (int64_t)nx * y + (int64_t)z * plane;
+                        const uint32_t wd = (SPECIAL && slot >= 0) ? word[node] : 0u;
+                        if (wd == 0u) {
+                            Mom m;
+                            gather_evaluate<TY>(eup, efl, dn, col, p0, pp5, c6, m);
+                            if (diag) {
+                                dm += m.rho - rho0;
+                                de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
+                            }
+                            collide(m, omega);
+                            store_mom<S>(dst, ai, m, rho0, sc);
+                        } else if constexpr (SPECIAL) {
+                            float fw[27];
+                            gather_all<TY>(eup, efl, dn, col, p0, pp5, c6, fw);
+                            Mom ms;
+                            const int code = special_node<S, TY>(ga, parity, force != nullptr, wd, fw, x, y, z, node,
+                                                                 slot, x0, y0, ms);
+                            if (code) store_mom<S>(dst, ai, ms, rho0, sc);
+                            if (code == 2 && diag) {
+                                dm += ms.rho - rho0;
+                                de += 0.5f * (ms.ux * ms.ux + ms.uy * ms.uy + ms.uz * ms.uz);
+                            }
+                        }
+                    }
+                    if (k + 2 <= last) nb_arrive(3 + (k & 1), G::NTH);  // DONE(k)
+                }
                 pp5 = p5;
                 p5 = c5;
                 p0 = c0;
-                continue;
+                k3 = k3 == 2 ? 0 : k3 + 1;
+                k4 = (k4 + 1) & 3;
             }
-            // emit plane z (its down populations come from plane z+1, just written)
-            const int z = zs + k - 2;
-            __syncthreads();
-            if (own) {
-                const float *eup = smem + ((k - 2) % 3) * G::PLANE;  // plane z-1
-                const float *efl = smem + (3 + ((k - 1) & 1)) * G::PLANE;  // plane z
-                const int64_t ai = cxy + (int64_t)z * zst;
-                const int64_t node = (int64_t)x + (int64_t)nx * y + (int64_t)z * plane;
-                const uint32_t wd = (SPECIAL && slot >= 0) ? word[node] : 0u;
-                if (wd == 0u) {
-                    Mom m;
-                    gather_evaluate<TY>(eup, efl, dn, col, p0, pp5, c6, m);
-                    if (diag) {
-                        dm += m.rho - rho0;
-                        de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
+            if (diag) {
+                dmD += (double)dm;
+                deD += (double)de;
+            }
+        } else {
+            for (int k = 0; k <= last; ++k) {
+                if (k >= 4) nb_sync(3 + (k & 1), G::NTH);  // DONE(k-2): ring slots of plane k are free
+                if (active) {
+                    float cur[10];
+#pragma unroll
+                    for (int i = 0; i < 10; ++i) cur[i] = pre[i];
+                    if (k < last) {
+                        load_raw<S>(src, cxy + (int64_t)zn * zst, pre);
+                        zn = zn + 1 == nz ? 0 : zn + 1;
                     }
-                    collide(m, omega);
-                    store_mom<S>(dst, ai, m, rho0, sc);
-                } else if constexpr (SPECIAL) {
-                    float fw[27];
-                    gather_all<TY>(eup, efl, dn, col, p0, pp5, c6, fw);
-                    Mom ms;
-                    const int code =
-                        special_node<S, TY>(ga, parity, force != nullptr, wd, fw, x, y, z, node, slot, x0, y0, ms);
-                    if (code) store_mom<S>(dst, ai, ms, rho0, sc);
-                    if (code == 2 && diag) {
-                        dm += ms.rho - rho0;
-                        de += 0.5f * (ms.ux * ms.ux + ms.uy * ms.uy + ms.uz * ms.uz);
-                    }
+                    arrive_rim<S, TY>(cur, rho0, sc, rside, up_base + k4 * G::PLANE, fl_base + k3 * G::PLANE,
+                                      dn_base + (k & 1) * G::PLANE, ccol);
                 }
+                if (k >= 2) nb_arrive(1 + (k & 1), G::NTH);  // FULL(k)
+                k3 = k3 == 2 ? 0 : k3 + 1;
+                k4 = (k4 + 1) & 3;
             }
-            __syncthreads();
-            pp5 = p5;
-            p5 = c5;
-            p0 = c0;
         }
-        if (diag) {
-            dmD += (double)dm;
-            deD += (double)de;
-        }
+        __syncthreads();  // the next item reuses the rings from slot 0
     }
 
     if (diag) {
