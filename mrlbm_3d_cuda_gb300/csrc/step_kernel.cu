@@ -160,67 +160,54 @@ __device__ __forceinline__ float pull(const float *up, const float *fl, const fl
     }
 }
 
-struct Sums {
-    float rho, jx, jy, jz, sxx, syy, szz, sxy, sxz, syz;
+// Zeroth, first and second (c_x, c_y) sums of the 3 x 3 populations of one c_z class, from
+// row sums (by c_y) and column sums (by c_x): 19 additions instead of one per term.
+struct ClassSums {
+    float s0, sx, sy, sxx, syy, sxy;
 };
-
-// Add the opposite pair (q, opp q) with values a = f_q, b = f_opp to the moment sums.
-template <int Q>
-__device__ __forceinline__ void add_pair(float a, float b, Sums &s) {
-    constexpr int cx = cxq(Q), cy = cyq(Q), cz = czq(Q);
-    const float e = a + b, d = a - b;
-    s.rho += e;
-    if constexpr (cx > 0) s.jx += d;
-    if constexpr (cx < 0) s.jx -= d;
-    if constexpr (cy > 0) s.jy += d;
-    if constexpr (cy < 0) s.jy -= d;
-    if constexpr (cz > 0) s.jz += d;
-    if constexpr (cz < 0) s.jz -= d;
-    if constexpr (cx != 0) s.sxx += e;
-    if constexpr (cy != 0) s.syy += e;
-    if constexpr (cz != 0) s.szz += e;
-    if constexpr (cx * cy > 0) s.sxy += e;
-    if constexpr (cx * cy < 0) s.sxy -= e;
-    if constexpr (cx * cz > 0) s.sxz += e;
-    if constexpr (cx * cz < 0) s.sxz -= e;
-    if constexpr (cy * cz > 0) s.syz += e;
-    if constexpr (cy * cz < 0) s.syz -= e;
+__device__ __forceinline__ ClassSums class_sums(float mm, float m0, float mp, float zm, float zz, float zp, float pm,
+                                                float p0, float pp) {
+    // arguments: f(c_x, c_y) with m = -1, z = 0, p = +1, named <c_x><c_y>
+    const float rp = (mp + zp) + pp, r0 = (m0 + zz) + p0, rm = (mm + zm) + pm;  // by c_y = +1, 0, -1
+    const float cp = (pm + p0) + pp, cm = (mm + m0) + mp;                       // by c_x = +1, -1
+    ClassSums s;
+    s.s0 = (rp + r0) + rm;
+    s.sx = cp - cm;
+    s.sxx = cp + cm;
+    s.sy = rp - rm;
+    s.syy = rp + rm;
+    s.sxy = (pp + mm) - (pm + mp);
+    return s;
 }
 
-template <int Q, int TY>
-__device__ __forceinline__ void add_pulled_pair(const float *up, const float *fl, const float *dn, int col, Sums &s) {
-    add_pair<Q>(pull<Q, TY>(up, fl, dn, col), pull<oppq(Q), TY>(up, fl, dn, col), s);
-}
-
-// Gather the pulled populations of the owner node and evaluate its moments on the fly.
+// Gather the pulled populations of the owner node and evaluate its moments on the fly,
+// class by class (c_z = +1 from plane z-1, 0 from z, -1 from z+1).
 template <int TY>
 __device__ __forceinline__ void gather_evaluate(const float *up, const float *fl, const float *dn, int col, float f0,
                                                 float f5, float f6, Mom &m) {
-    Sums s{f0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    add_pulled_pair<1, TY>(up, fl, dn, col, s);
-    add_pulled_pair<3, TY>(up, fl, dn, col, s);
-    add_pair<5>(f5, f6, s);
-    add_pulled_pair<7, TY>(up, fl, dn, col, s);
-    add_pulled_pair<13, TY>(up, fl, dn, col, s);
-    add_pulled_pair<9, TY>(up, fl, dn, col, s);
-    add_pulled_pair<11, TY>(up, fl, dn, col, s);
-    add_pulled_pair<15, TY>(up, fl, dn, col, s);
-    add_pulled_pair<17, TY>(up, fl, dn, col, s);
-    add_pulled_pair<19, TY>(up, fl, dn, col, s);
-    add_pulled_pair<21, TY>(up, fl, dn, col, s);
-    add_pulled_pair<23, TY>(up, fl, dn, col, s);
-    add_pulled_pair<25, TY>(up, fl, dn, col, s);
-    const float inv = 1.0f / s.rho;
-    m.rho = s.rho;
-    m.ux = s.jx * inv;
-    m.uy = s.jy * inv;
-    m.uz = s.jz * inv;
-    m.mxx = s.sxx * inv - kCs2;
-    m.myy = s.syy * inv - kCs2;
-    m.mzz = s.szz * inv - kCs2;
-    m.mxy = s.sxy * inv;
-    m.mxz = s.sxz * inv;
-    m.myz = s.syz * inv;
+#define MRLBM_P(q) pull<q, TY>(up, fl, dn, col)
+    // c_z = +1: (cx,cy) = (-1,-1) 22, (-1,0) 16, (-1,1) 25, (0,-1) 18, (0,0) 5, (0,1) 11, (1,-1) 23, (1,0) 9, (1,1) 19
+    const ClassSums u = class_sums(MRLBM_P(22), MRLBM_P(16), MRLBM_P(25), MRLBM_P(18), f5, MRLBM_P(11), MRLBM_P(23),
+                                   MRLBM_P(9), MRLBM_P(19));
+    // c_z = 0: 8, 2, 14, 4, 0, 3, 13, 1, 7
+    const ClassSums c = class_sums(MRLBM_P(8), MRLBM_P(2), MRLBM_P(14), MRLBM_P(4), f0, MRLBM_P(3), MRLBM_P(13),
+                                   MRLBM_P(1), MRLBM_P(7));
+    // c_z = -1: 20, 10, 24, 12, 6, 17, 26, 15, 21
+    const ClassSums d = class_sums(MRLBM_P(20), MRLBM_P(10), MRLBM_P(24), MRLBM_P(12), f6, MRLBM_P(17), MRLBM_P(26),
+                                   MRLBM_P(15), MRLBM_P(21));
+#undef MRLBM_P
+    const float rho = (u.s0 + c.s0) + d.s0;
+    const float inv = 1.0f / rho;
+    m.rho = rho;
+    m.ux = ((u.sx + c.sx) + d.sx) * inv;
+    m.uy = ((u.sy + c.sy) + d.sy) * inv;
+    m.uz = (u.s0 - d.s0) * inv;
+    m.mxx = ((u.sxx + c.sxx) + d.sxx) * inv - kCs2;
+    m.myy = ((u.syy + c.syy) + d.syy) * inv - kCs2;
+    m.mzz = (u.s0 + d.s0) * inv - kCs2;
+    m.mxy = ((u.sxy + c.sxy) + d.sxy) * inv;
+    m.mxz = (u.sx - d.sx) * inv;
+    m.myz = (u.sy - d.sy) * inv;
 }
 
 template <int TY>
@@ -361,9 +348,11 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
             }
         }
 
-        float pre[10];
+        // raw moments of planes k (being rebuilt) and k+1 (in flight); the two buffers swap
+        // roles every plane, so the plane loops are unrolled by two
+        float pa[10], pb[10];
         const int zm = zs == 0 ? nz - 1 : zs - 1;
-        if (active) load_raw<S>(src, cxy + (int64_t)zm * zst, pre);
+        if (active) load_raw<S>(src, cxy + (int64_t)zm * zst, pa);
         int zn = zs;  // plane of the next prefetch (wrapped)
         int k3 = 0, k4 = 0;  // k % 3, k % 4
 
@@ -371,16 +360,13 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
             float c0 = 0.f, c5 = 0.f, c6 = 0.f;   // own-column rest / up / down populations of plane k
             float p0 = 0.f, p5 = 0.f, pp5 = 0.f;  // f0(k-1), f5(k-1), f5(k-2)
             float dm = 0.f, de = 0.f;
-            for (int k = 0; k <= last; ++k) {
+            auto owner_plane = [&](const int k, const float (&cur)[10], float (&nxt)[10]) {
                 float *up = up_base + k4 * G::PLANE;
                 float *flt = fl_base + k3 * G::PLANE;
                 float *dn = dn_base + (k & 1) * G::PLANE;
                 if (own) {
-                    float cur[10];
-#pragma unroll
-                    for (int i = 0; i < 10; ++i) cur[i] = pre[i];
                     if (k < last) {
-                        load_raw<S>(src, cxy + (int64_t)zn * zst, pre);
+                        load_raw<S>(src, cxy + (int64_t)zn * zst, nxt);
                         zn = zn + 1 == nz ? 0 : zn + 1;
                     }
                     arrive_own<S, TY>(cur, rho0, sc, up, flt, dn, col, c0, c5, c6);
@@ -423,20 +409,21 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 p0 = c0;
                 k3 = k3 == 2 ? 0 : k3 + 1;
                 k4 = (k4 + 1) & 3;
+            };
+            for (int k = 0; k <= last; k += 2) {
+                owner_plane(k, pa, pb);
+                if (k + 1 <= last) owner_plane(k + 1, pb, pa);
             }
             if (diag) {
                 dmD += (double)dm;
                 deD += (double)de;
             }
         } else {
-            for (int k = 0; k <= last; ++k) {
+            auto rim_plane = [&](const int k, const float (&cur)[10], float (&nxt)[10]) {
                 if (k >= 4) nb_sync(3 + (k & 1), G::NTH);  // DONE(k-2): ring slots of plane k are free
                 if (active) {
-                    float cur[10];
-#pragma unroll
-                    for (int i = 0; i < 10; ++i) cur[i] = pre[i];
                     if (k < last) {
-                        load_raw<S>(src, cxy + (int64_t)zn * zst, pre);
+                        load_raw<S>(src, cxy + (int64_t)zn * zst, nxt);
                         zn = zn + 1 == nz ? 0 : zn + 1;
                     }
                     arrive_rim<S, TY>(cur, rho0, sc, rside, up_base + k4 * G::PLANE, fl_base + k3 * G::PLANE,
@@ -445,6 +432,10 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 if (k >= 2) nb_arrive(1 + (k & 1), G::NTH);  // FULL(k)
                 k3 = k3 == 2 ? 0 : k3 + 1;
                 k4 = (k4 + 1) & 3;
+            };
+            for (int k = 0; k <= last; k += 2) {
+                rim_plane(k, pa, pb);
+                if (k + 1 <= last) rim_plane(k + 1, pb, pa);
             }
         }
         __syncthreads();  // the next item reuses the rings from slot 0
