@@ -193,6 +193,26 @@ int mrlbm_checkpoint_save(mrlbm_handle *h, const char *path); /* restart.bin lay
 int mrlbm_checkpoint_load(mrlbm_handle *h, const char *path);
 int mrlbm_write_vti(mrlbm_handle *h, const char *path);       /* data<10000000+it>.vti layout */
 
+/* ---- allocation-free step (no counterpart in the reference) ------------------------------------
+ * One time step of a fully periodic box (no walls, no inlet / outlet) from m_in to m_out,
+ * for callers that cannot allocate device memory: it calls no cudaMalloc / cudaFree and no
+ * allocating library routine.  The step kernel's scratch (argument block, work items,
+ * diagnostics partials) is one fixed 64 KiB array in the library's device image, which
+ * bounds the grid to at most 11776 xy tiles of 32 x 16 nodes (ceil(nx/32) * ceil(ny/16)),
+ * e.g. 2048 x 2944 nodes per z plane; larger grids are rejected with MRLBM_ERR_INVALID_ARG.
+ * Every call shares that array and it keeps the last call's contents (each call rewrites
+ * what it reads and clears its error word); calls that overlap on the GPU (two streams or
+ * two host threads) race on it.
+ * m_in / m_out: device pointers, 16-byte aligned, not overlapping, FP32 moments in the
+ * solver's storage layout: field f of node (x, y, z) at element
+ * (((z*ny + y)*ceil(nx/32) + x/32)*10 + f)*32 + x%32, fields in the order of
+ * MRLBM_FIELD_* with field 0 holding rho - rho0; nz*ny*ceil(nx/32)*320 floats each.
+ * Grid: positive multiples of 8 x 8 x 4.  diag: NULL, or {mass, kinetic energy} as
+ * mrlbm_get_diagnostics, in which case the call waits for the step.  Otherwise it is
+ * asynchronous on `cuda_stream` (a cudaStream_t; NULL = default stream). */
+int mrlbm_step_periodic_noalloc(const float *m_in, float *m_out, int32_t nx, int32_t ny, int32_t nz, float omega,
+                                float rho0, double *diag, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -726,4 +726,22 @@ int mrlbm_write_vti(mrlbm_handle *h, const char *path) {
     return fail(h, MRLBM_ERR_UNSUPPORTED, "vti writer not built yet");
 }
 
+int mrlbm_step_periodic_noalloc(const float *m_in, float *m_out, int32_t nx, int32_t ny, int32_t nz, float omega,
+                                float rho0, double *diag, void *cuda_stream) {
+    NoAllocStep p;
+    p.m_in = m_in;
+    p.m_out = m_out;
+    p.nx = nx;
+    p.ny = ny;
+    p.nz = nz;
+    p.omega = omega;
+    p.rho0 = rho0;
+    p.diag_host = diag;
+    p.stream = (cudaStream_t)cuda_stream;
+    std::string err;
+    const int rc = noalloc_periodic_step(p, err);
+    if (rc != MRLBM_OK) return fail(nullptr, rc, err);
+    return MRLBM_OK;
+}
+
 }  // extern "C"

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 
 #include <cuda_runtime.h>
 
@@ -94,5 +95,33 @@ cudaError_t launch_init(const InitArgs &a, int storage, cudaStream_t s);
 cudaError_t launch_convert(const void *src, void *dst_a, void *dst_b, float *f32, uint32_t field_mask,
                            int layout, int nx, int ny, int nz, int storage, const StorageScale &sc, int dir,
                            cudaStream_t s);
+
+// Allocation-free periodic step (mrlbm_step_periodic_noalloc).  Everything the step kernel
+// needs besides the caller's two moment buffers lives in one fixed array in the library's
+// device image, laid out as:
+//   [0, 1536)            StepArgs
+//   [1536, 1552)         mass / energy sums (2 doubles)
+//   [1600, 1604)         error word
+//   [2048, 18432)        per-CTA diagnostics partials, 2 doubles per CTA
+//   [18432, 65536)       work items, one int32 each
+constexpr int kNoAllocScratchBytes = 64 * 1024;
+constexpr int kNoAllocDiagOffset = 1536;
+constexpr int kNoAllocErrorOffset = 1600;
+constexpr int kNoAllocPartOffset = 2048;
+constexpr int kNoAllocMaxCtas = 1024;
+constexpr int kNoAllocItemsOffset = kNoAllocPartOffset + kNoAllocMaxCtas * 2 * (int)sizeof(double);
+constexpr int kNoAllocMaxItems = (kNoAllocScratchBytes - kNoAllocItemsOffset) / (int)sizeof(int32_t);  // 11776
+constexpr int kNoAllocTileY = 16;
+
+struct NoAllocStep {
+    const float *m_in = nullptr;  // FP32 moments in the x-blocked storage layout
+    float *m_out = nullptr;
+    int nx = 0, ny = 0, nz = 0;
+    float omega = 0.f, rho0 = 1.f;
+    double *diag_host = nullptr;  // optional: {mass, kinetic energy} as mrlbm_get_diagnostics
+    cudaStream_t stream = nullptr;
+};
+// Returns an MRLBM_* status; on failure `err` holds the message.
+int noalloc_periodic_step(const NoAllocStep &p, std::string &err);
 
 }  // namespace mrlbm

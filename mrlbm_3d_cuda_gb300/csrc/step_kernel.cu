@@ -14,7 +14,11 @@
 // (neighbour moments read through L2) into shared-memory ring buffers split by c_z, so a
 // node's 27 pulled populations come from planes z-1, z, z+1 without any population array in
 // HBM.  Post-collision moments go to the second ping-pong buffer.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
+#include <mutex>
+#include <string>
 
 #include "mrlbm_internal.h"
 #include "storage.cuh"
@@ -563,6 +567,168 @@ int step_kernel_max_ctas_per_sm(int storage, int tile_y) {
         case MRLBM_STORAGE_BF16: return occ_s<__nv_bfloat16>(tile_y);
         default: return 0;
     }
+}
+
+// ---- allocation-free periodic step --------------------------------------------------------
+// For callers that cannot allocate device memory: the step kernel's own scratch (its argument
+// block, work-item list, diagnostics partials and sums, error word) lives in this fixed array
+// of the library's device image, kNoAllocScratchBytes = 64 KiB, laid out as in kernels.h.
+// Every call shares it and it keeps the last call's contents; calls that overlap on the GPU
+// (two streams, or two host threads) race on it.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static_assert(sizeof(StepArgs) <= kNoAllocDiagOffset, "StepArgs outgrew its scratch slot");
+static_assert(kNoAllocItemsOffset < kNoAllocScratchBytes, "scratch layout");
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Write the argument block, clear the error word and fill the work items (every xy tile of
+// every z segment, segment-major) inside the scratch array: one launch, no host staging.
+__global__ void noalloc_setup_kernel(const StepArgs a, unsigned char *scratch, int tiles, int n_items) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        *(StepArgs *)scratch = a;
+        *(int *)(scratch + kNoAllocErrorOffset) = 0;
+    }
+    int32_t *items = (int32_t *)(scratch + kNoAllocItemsOffset);
+    for (int j = i; j < n_items; j += gridDim.x * blockDim.x) items[j] = (j % tiles) | ((j / tiles) << 20);
+}
+
+// Device address of the scratch array on the current device, looked up once per device.
+cudaError_t noalloc_scratch(int dev, unsigned char **out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = (unsigned char *)g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+
+int noalloc_cuda_fail(cudaError_t e, const char *what, std::string &err) {
+    err = std::string("mrlbm_step_periodic_noalloc: ") + what + ": " + cudaGetErrorString(e);
+    return e == cudaErrorNoKernelImageForDevice ? MRLBM_ERR_UNSUPPORTED : MRLBM_ERR_CUDA;
+}
+
+}  // namespace
+
+int noalloc_periodic_step(const NoAllocStep &p, std::string &err) {
+    const char *fn = "mrlbm_step_periodic_noalloc: ";
+    // host-side checks first: nothing below runs for a rejected call
+    if (!p.m_in || !p.m_out) {
+        err = std::string(fn) + "null moment buffer";
+        return MRLBM_ERR_INVALID_ARG;
+    }
+    if (p.nx <= 0 || p.ny <= 0 || p.nz <= 0 || p.nx % 8 || p.ny % 8 || p.nz % 4) {
+        err = std::string(fn) + "grid must be positive multiples of 8 x 8 x 4";
+        return MRLBM_ERR_INVALID_ARG;
+    }
+    if ((int64_t)p.nx * p.ny * p.nz >= (1LL << 31) * 8) {
+        err = std::string(fn) + "grid too large";
+        return MRLBM_ERR_INVALID_ARG;
+    }
+    if (!(p.omega > 0.f && p.omega < 2.f) || !(p.rho0 > 0.f) || !std::isfinite(p.rho0)) {
+        err = std::string(fn) + "need 0 < omega < 2 and rho0 > 0";
+        return MRLBM_ERR_INVALID_ARG;
+    }
+    if ((uintptr_t)p.m_in % 16 || (uintptr_t)p.m_out % 16) {
+        err = std::string(fn) + "moment buffers must be 16-byte aligned";
+        return MRLBM_ERR_INVALID_ARG;
+    }
+    const int64_t bytes = aos_elements(p.nx, p.ny, p.nz) * (int64_t)sizeof(float);
+    const uintptr_t a = (uintptr_t)p.m_in, b = (uintptr_t)p.m_out;
+    if ((a <= b ? b - a : a - b) < (uint64_t)bytes) {
+        err = std::string(fn) + "input and output moment buffers overlap";
+        return MRLBM_ERR_INVALID_ARG;
+    }
+    const int tiles_x = (p.nx + TILE_X - 1) / TILE_X, tiles_y = (p.ny + kNoAllocTileY - 1) / kNoAllocTileY;
+    const int tiles = tiles_x * tiles_y;
+    if (tiles > kNoAllocMaxItems) {
+        err = std::string(fn) + "grid too large for the fixed 64 KiB scratch: " + std::to_string(tiles) +
+              " xy tiles of 32 x 16 nodes, at most " + std::to_string(kNoAllocMaxItems);
+        return MRLBM_ERR_INVALID_ARG;
+    }
+
+    int dev = 0, major = 0, minor = 0, n_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return noalloc_cuda_fail(e, "cudaGetDevice", err);
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        err = std::string(fn) + "device ordinal out of range";
+        return MRLBM_ERR_UNSUPPORTED;
+    }
+    if ((e = cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+        return noalloc_cuda_fail(e, "cudaDeviceGetAttribute", err);
+    if (!(major == 10 && minor == 3)) {
+        err = std::string(fn) + "libmrlbm is built for sm_103a (GB300) only";
+        return MRLBM_ERR_UNSUPPORTED;
+    }
+    unsigned char *scratch = nullptr;
+    if ((e = noalloc_scratch(dev, &scratch)) != cudaSuccess) return noalloc_cuda_fail(e, "cudaGetSymbolAddress", err);
+
+    // tiling: 32 x 16 columns; the longest z segment that still gives every resident CTA
+    // several items, lengthened if the item list would not fit the scratch
+    const int per_sm = std::max(1, occ_s<float>(kNoAllocTileY));
+    const int resident = per_sm * n_sm;
+    int lz = p.nz;
+    while (lz > 16 && (int64_t)tiles * ((p.nz + lz - 1) / lz) < 4LL * resident) lz = (lz + 1) / 2;
+    const int max_seg = kNoAllocMaxItems / tiles;
+    if ((p.nz + lz - 1) / lz > max_seg) lz = (p.nz + max_seg - 1) / max_seg;
+    const int nseg = (p.nz + lz - 1) / lz;
+    const int n_items = tiles * nseg;
+    const int n_ctas = std::max(1, std::min(std::min(n_items, resident), kNoAllocMaxCtas));
+
+    StepArgs sa;
+    sa.m[0] = const_cast<float *>(p.m_in);
+    sa.m[1] = p.m_out;
+    sa.nxb = (p.nx + kXBlock - 1) / kXBlock;
+    sa.items = (const int32_t *)(scratch + kNoAllocItemsOffset);
+    sa.n_items = n_items;
+    sa.nx = p.nx;
+    sa.ny = p.ny;
+    sa.nz = p.nz;
+    sa.tiles_x = tiles_x;
+    sa.tiles_y = tiles_y;
+    sa.tile_y = kNoAllocTileY;
+    sa.lz = lz;
+    sa.omega = p.omega;
+    sa.rho0 = p.rho0;
+    for (int k = 0; k < 3; ++k) sa.sc.s[k] = sa.sc.is[k] = 1.f;
+    sa.error = (int *)(scratch + kNoAllocErrorOffset);
+
+    noalloc_setup_kernel<<<(n_items + 255) / 256, 256, 0, p.stream>>>(sa, scratch, tiles, n_items);
+    if ((e = cudaGetLastError()) != cudaSuccess) return noalloc_cuda_fail(e, "set-up launch", err);
+    StepLaunch L;
+    L.ga = (const StepArgs *)scratch;
+    L.parity = 0;
+    L.n_ctas = n_ctas;
+    double *part = (double *)(scratch + kNoAllocPartOffset);
+    double *sums = (double *)(scratch + kNoAllocDiagOffset);
+    if (p.diag_host) L.diag_part = part;
+    if ((e = launch_t<float, kNoAllocTileY, false>(L, p.stream)) != cudaSuccess)
+        return noalloc_cuda_fail(e, "step launch", err);
+    if (p.diag_host) {
+        if ((e = launch_diag_finalize(part, n_ctas, sums, p.stream)) != cudaSuccess)
+            return noalloc_cuda_fail(e, "diagnostics launch", err);
+        double v[2];
+        if ((e = cudaMemcpyAsync(v, sums, sizeof(v), cudaMemcpyDeviceToHost, p.stream)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(p.stream)) != cudaSuccess)
+            return noalloc_cuda_fail(e, "diagnostics read-back", err);
+        p.diag_host[0] = (double)p.nx * p.ny * p.nz * p.rho0 + v[0];
+        p.diag_host[1] = v[1];
+        if (!std::isfinite(v[0]) || !std::isfinite(v[1])) {
+            err = std::string(fn) + "mass / energy diagnostics are not finite";
+            return MRLBM_ERR_DIVERGED;
+        }
+    }
+    return MRLBM_OK;
 }
 
 }  // namespace mrlbm

@@ -97,6 +97,8 @@ _SIGS = {
     "mrlbm_checkpoint_save": (C.c_int, [C.c_void_p, C.c_char_p]),
     "mrlbm_checkpoint_load": (C.c_int, [C.c_void_p, C.c_char_p]),
     "mrlbm_write_vti": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "mrlbm_step_periodic_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float,
+                                              C.c_float, C.c_void_p, C.c_void_p]),
 }
 
 EXPORTED = tuple(_SIGS)
