@@ -34,6 +34,18 @@ B_MIN = {"f32": 80.0, "f16": 40.0, "bf16": 40.0}    # moments in + out only
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
 
 
+def measured_traffic(storage: str):
+    """DRAM bytes per node of the step kernel from the committed ncu summary, or None."""
+    p = ROOT / "profiles" / "dram_traffic.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        parts = line.split()
+        if len(parts) >= 3 and not line.startswith("#") and parts[0] == "step_kernel" and parts[1] == storage:
+            return float(parts[2])
+    return None
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -48,7 +60,7 @@ class ClockSampler:
     def __init__(self, index: int = 0):
         self.index = index
         self.rows = []
-        self._stop = threading.Event()
+        self._first = threading.Event()
         self._proc = None
 
     def __enter__(self):
@@ -62,6 +74,10 @@ class ClockSampler:
             threading.Thread(target=self._read, daemon=True).start()
         except (OSError, FileNotFoundError):
             self._proc = None
+        # nvidia-smi needs a moment before its first sample: start timing only once it samples
+        t0 = time.time()
+        while self._proc and not self._first.is_set() and time.time() - t0 < 5.0:
+            self._first.wait(0.05)
         return self
 
     def _read(self):
@@ -69,6 +85,7 @@ class ClockSampler:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 7:
                 self.rows.append(parts)
+                self._first.set()
 
     def __exit__(self, *exc):
         if self._proc:
@@ -115,26 +132,45 @@ def cpu_baseline(n: int, slab: int, steps: int, bits: int = 32):
                       f"FP{bits} restatement, OpenMP {cores} threads"}
 
 
+def metric_name(n: int) -> str:
+    return f"MLUPS (D3Q27 MR-LBM, {n}^3 Taylor-Green)"
+
+
 def run_reference(args):
+    """The reference's algorithm on the host cores: the oracle (the reference has no CPU
+    path), one bounded n x n x slab piece of the same Taylor-Green field per step."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
+    import oracle
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
     n = args.n
     slab = max(4, args.ref_slab)
-    res = None
-    vals = []
+    desc = cases.periodic_box(n, n, slab, u0=0.05, re=1600.0, length=n / (2 * math.pi))
+    o = oracle.Oracle(desc, 32)
+    o.init(N.INIT_TAYLOR_GREEN, (0.05, n / (2 * math.pi)))
     for _ in range(args.warmup):
-        cpu_baseline(n, slab, 1)
+        o.step(1)
+    times = []
     for _ in range(args.steps):
-        res = cpu_baseline(n, slab, 1)
-        vals.append(res["value"])
-    value = float(np.median(vals)) if vals else 0.0
+        t0 = time.perf_counter()
+        o.step(1)
+        times.append(time.perf_counter() - t0)
+    o.close()
+    total = sum(times)
+    value = n * n * slab * len(times) / total / 1e6 if total > 0 else 0.0
+    cores = os.cpu_count() or 1
     line = {
-        "impl": "reference", "metric": "MLUPS (D3Q27 MR-LBM, 256^3 Taylor-Green)", "value": value, "unit": "MLUPS",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "impl": "reference", "metric": metric_name(n), "value": value, "unit": "MLUPS",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / max(1, len(times)), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"taylor-green {n}^3 D3Q27, u0=0.05, Re=1600", "storage": "f32"},
-        "cpu_baseline": {**res, "value": value} if res else None,
+        "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": cores, "kind": "port",
+                         "sample": f"each step: one step of a {n}x{n}x{slab} periodic slab of the same "
+                                   f"Taylor-Green field, FP32 restatement of the reference step, "
+                                   f"OpenMP {cores} threads"},
         "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -209,7 +245,7 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     achieved = n_nodes * B_ALG[storage] / (kernel_ms * 1e-3) / 1e9
     line = {
-        "metric": "MLUPS (D3Q27 MR-LBM, 256^3 Taylor-Green)" if args.n == 256 else f"MLUPS (D3Q27 MR-LBM, {args.n}^3 TGV)",
+        "metric": metric_name(args.n),
         "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": storage, "data": "synthetic",
@@ -221,7 +257,8 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "bytes_per_lup": B_ALG[storage],
                      "frac_vs_min_traffic": n_nodes * B_MIN[storage] / (kernel_ms * 1e-3) / 1e9 / peak,
-                     "traffic": None},
+                     "traffic": (measured_traffic(storage) * n_nodes if measured_traffic(storage) else None),
+                     "traffic_source": "ncu dram__bytes_read+write per node (profiles/dram_traffic.txt) x nodes"},
         "e2e": {"value": e2e_value, "unit": "MLUPS", "h2d_bytes_per_step": hv.nbytes / e2e_steps,
                 "d2h_bytes_per_step": 16 + hv.nbytes / e2e_steps},
         "gpu_launches": args.steps,
@@ -239,7 +276,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f32", choices=list(STORAGE))
