@@ -187,13 +187,25 @@ def run_ours(args):
     from mrlbm_3d_cuda_gb300 import native as N
 
     storage = args.storage
-    desc = cases.c2_taylor_green(args.n, STORAGE[storage])
+    cyl = args.workload == "cylinder"
+    if cyl:
+        desc = cases.reference_cylinder(STORAGE[storage], args.diameter)
+        workload = (f"reference cylinder case scaled to D={args.diameter}: {desc.nx}x{desc.ny}x{desc.nz} D3Q27, "
+                    f"Re=100, U=0.1, convective outlet, periodic y/z, {storage} moment storage")
+        metric = f"MLUPS (D3Q27 MR-LBM, cylinder D={args.diameter} {desc.nx}x{desc.ny}x{desc.nz})"
+    else:
+        desc = cases.c2_taylor_green(args.n, STORAGE[storage])
+        workload = f"taylor-green {args.n}^3 D3Q27, u0=0.05, Re=1600, {storage} moment storage"
+        metric = metric_name(args.n)
     n_nodes = desc.nx * desc.ny * desc.nz
     stream = torch.cuda.Stream()  # a real stream handle: the library launches on it, events time it
     torch.cuda.set_stream(stream)
     sim = Simulation(desc, init=False)
     sim.set_stream(stream.cuda_stream)
-    sim.init(N.INIT_TAYLOR_GREEN, cases.tgv_params(desc))
+    if cyl:
+        sim.init(N.INIT_REFERENCE_NOISE)
+    else:
+        sim.init(N.INIT_TAYLOR_GREEN, cases.tgv_params(desc))
     info = sim.get_info()
 
     def barrier():
@@ -245,11 +257,11 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     achieved = n_nodes * B_ALG[storage] / (kernel_ms * 1e-3) / 1e9
     line = {
-        "metric": metric_name(args.n),
+        "metric": metric,
         "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": storage, "data": "synthetic",
-        "config": {"workload": f"taylor-green {args.n}^3 D3Q27, u0=0.05, Re=1600, {storage} moment storage",
+        "config": {"workload": workload,
                    "storage": storage, "tile": list(info.tile), "ctas": int(info.reserved[0]),
                    "l2": f"inputs larger than L2 ({n_nodes * 10 * (4 if storage == 'f32' else 2) / 1e6:.0f} MB "
                          f"per moment buffer vs 129 MB L2)",
@@ -261,7 +273,7 @@ def run_ours(args):
                      "traffic_source": "ncu dram__bytes_read+write per node (profiles/dram_traffic.txt) x nodes"},
         "e2e": {"value": e2e_value, "unit": "MLUPS", "h2d_bytes_per_step": hv.nbytes / e2e_steps,
                 "d2h_bytes_per_step": 16 + hv.nbytes / e2e_steps},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * (2 if cyl else 1),  # step kernel (+ wall kernel)
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -281,6 +293,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f32", choices=list(STORAGE))
     ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder"])
+    ap.add_argument("--diameter", type=int, default=16)
     ap.add_argument("--ref-slab", type=int, default=8)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")

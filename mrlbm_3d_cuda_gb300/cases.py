@@ -15,10 +15,22 @@ def _finish(d: N.CaseDesc, storage: int = N.STORAGE_F32) -> N.CaseDesc:
     return N.finalize(d)
 
 
-def reference_cylinder(storage: int = N.STORAGE_F32) -> N.CaseDesc:
+def reference_cylinder(storage: int = N.STORAGE_F32, diameter: int = 16) -> N.CaseDesc:
     """The reference's shipped cylinder case (cases/cylinder/constants.cuh:8-54):
-    336 x 144 x 48, D = 16 at (71.5, 71.5), Re = 100, U = 0.1, periodic y and z, convective outlet."""
-    return _finish(N.default_desc(N.GEOM_CYLINDER), storage)
+    336 x 144 x 48, D = 16 at (71.5, 71.5), Re = 100, U = 0.1, periodic y and z, convective outlet.
+    `diameter` rescales it as the reference's constants do when D is edited: LW = LN = LS = 4D,
+    LE = 16D, NZ = 3D, centre LW + (D - 1) / 2, classification box +-4 nodes around the body."""
+    d = N.default_desc(N.GEOM_CYLINDER)
+    if diameter != 16:
+        D = int(diameter)
+        lw, le, ln = 4 * D, 16 * D, 4 * D
+        d.nx, d.ny, d.nz = lw + D + le, 2 * ln + D, 3 * D
+        d.d_wall[0] = float(D)
+        d.xc = d.yc = lw + 0.5 * (D - 1)
+        d.scan_box[0], d.scan_box[1], d.scan_box[2], d.scan_box[3] = lw - 4, lw + D + 4, ln - 4, ln + D + 4
+        if d.length > 0:
+            d.length = float(D)
+    return _finish(d, storage)
 
 
 def reference_annulus(storage: int = N.STORAGE_F32) -> N.CaseDesc:

@@ -1,0 +1,70 @@
+"""Golden vectors from a run of the reference's own GPU build (sakthi-lbm/MRLBM_3D_CUDA).
+
+The reference ships no test data, so the time step is pinned against its own solver run on
+a GB300: `oracle/ref_gpu.py` stages, builds and runs the shipped cylinder case
+(cases/cylinder/constants.cuh: 336 x 144 x 48, D = 16, Re = 100, U = 0.1, periodic y and z,
+convective outlet) for MAX_ITER = N, i.e. iterations 0..N = N + 1 steps from the reference
+initial state.  Its checkpoint (restart.bin, MRLBM_3D/src/restart/restart_io.cu:3-52:
+int iteration, then rho - rho0, ux, uy, uz, mxx, myy, mzz, mxy, mxz, myz, each NX*NY*NZ
+floats in the tiled IDX_BLOCK order) and forces.dat (stat_header.cuh:16-33: `iter Fx Fy Fz`
+per step) are reduced here to a fixture small enough to commit:
+  * every node that is not plain bulk fluid (walls, BCFLUID, inlet / outlet faces) plus a
+    seeded random sample of 40,000 nodes, all 10 moments, by tiled index;
+  * per-field max |m|, sum m and sum m^2 over the whole grid (FP64);
+  * the forces.dat rows.
+
+Run on the GPU machine from the repository root:
+    python oracle/ref_gpu.py stage cyl_n10 --steps 10          (where the reference tree is)
+    python oracle/ref_gpu.py check && python oracle/ref_gpu.py build cyl_n10 && python oracle/ref_gpu.py run cyl_n10
+    python tests/golden/make_ref_run_golden.py cyl_n10 tests/golden/ref_cylinder_run_n10.npz
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+N_RANDOM = 40000
+
+
+def read_restart(path: Path, n: int):
+    raw = path.read_bytes()
+    it = int(np.frombuffer(raw[:4], dtype=np.int32)[0])
+    m = np.frombuffer(raw[4:4 + 40 * n], dtype=np.float32).reshape(10, n)
+    return it, m
+
+
+def main(tag: str, out: str):
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    d = ROOT / "baseline" / "_ref" / tag
+    cfg = json.loads((d / "config.json").read_text())
+    if cfg["diameter"] != 16:
+        raise SystemExit("fixtures are made for the shipped D = 16 case only")
+    desc = cases.reference_cylinder()
+    n = desc.nx * desc.ny * desc.nz
+    restart = next((d / "run").rglob("restart.bin"))
+    forces = np.loadtxt(next((d / "run").rglob("forces.dat")), ndmin=2)
+    it, m = read_restart(restart, n)
+    assert it == cfg["steps"] + 1, (it, cfg)
+    sim = Simulation(desc, host_only=True)
+    types = sim.node_types(layout=N.LAYOUT_REF_TILED)
+    sim.close()
+    special = np.flatnonzero((types >> 20) != 0)
+    rng = np.random.default_rng(20261203)
+    idx = np.union1d(special, rng.choice(n, N_RANDOM, replace=False)).astype(np.int64)
+    m64 = m.astype(np.float64)
+    np.savez_compressed(
+        out, steps=np.int64(it), idx=idx.astype(np.int32), moments=m[:, idx],
+        field_max=np.abs(m64).max(axis=1), field_sum=m64.sum(axis=1), field_sumsq=(m64 * m64).sum(axis=1),
+        forces=forces, nxyz=np.array([desc.nx, desc.ny, desc.nz], dtype=np.int32))
+    print(f"{out}: {it} steps, {idx.size} sampled nodes, {forces.shape[0]} force rows")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1], sys.argv[2])
