@@ -47,6 +47,12 @@ struct mrlbm_handle {
     int32_t *d_items = nullptr, *d_tile_slot = nullptr;
     float *d_side = nullptr;
     int n_special = 0;
+    // non-bulk node list handled by the node-list kernel
+    uint64_t *d_list_xyz = nullptr;
+    uint32_t *d_list_word = nullptr;
+    int32_t *d_row_base = nullptr;
+    float *d_popbuf = nullptr;
+    int n_list_pop = 0, n_list = 0, n_list_blocks = 0;
     // walls
     float *d_wf[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
     uint32_t *d_wm[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
@@ -107,6 +113,10 @@ void free_all(mrlbm_handle *h) {
     f(h->d_items);
     f(h->d_tile_slot);
     f(h->d_side);
+    f(h->d_list_xyz);
+    f(h->d_list_word);
+    f(h->d_row_base);
+    f(h->d_popbuf);
     for (int w = 0; w < 2; ++w) {
         for (int k = 0; k < 3; ++k) f(h->d_wf[w][k]);
         for (int k = 0; k < 2; ++k) f(h->d_wm[w][k]);
@@ -350,6 +360,47 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
         else if (special) slot[t] = n_special++;
     }
     h->n_special = n_special;
+
+    // Non-bulk nodes of special tiles, in the order the step kernel exports their pulled
+    // populations: slot, z, tile row, x.  Solid nodes of updated blocks need no populations
+    // and follow the others; frozen nodes are never updated and are in no list.
+    std::vector<uint64_t> list_xyz;
+    std::vector<uint32_t> list_word;
+    std::vector<int32_t> row_base((size_t)n_special * d.nz * h->tile_y, 0);
+    std::vector<uint64_t> solid_xyz;
+    std::vector<uint32_t> solid_word;
+    for (int t = 0; t < tiles; ++t) {
+        if (slot[t] < 0) continue;
+        const int x0 = (t % h->tiles_x) * TILE_X, y0 = (t / h->tiles_x) * h->tile_y;
+        for (int z = 0; z < d.nz; ++z)
+            for (int r = 0; r < h->tile_y; ++r) {
+                row_base[((size_t)slot[t] * d.nz + z) * h->tile_y + r] = (int32_t)list_xyz.size();
+                const int y = y0 + r;
+                if (y >= d.ny) continue;
+                for (int x = x0; x < std::min(d.nx, x0 + TILE_X); ++x) {
+                    const int64_t i = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
+                    const uint32_t wd = word[i];
+                    if (wd == 0u || (wd & NW_FROZEN)) continue;
+                    const uint64_t p = (uint64_t)x | ((uint64_t)y << 21) | ((uint64_t)z << 42);
+                    if ((wd & NW_CLASS_MASK) == C_SOLID) {
+                        solid_xyz.push_back(p);
+                        solid_word.push_back(wd);
+                    } else {
+                        list_xyz.push_back(p);
+                        list_word.push_back(wd);
+                    }
+                }
+            }
+    }
+    if (list_xyz.size() + solid_xyz.size() >= (size_t)INT32_MAX / 27) {
+        free_all(h.get());
+        return fail(nullptr, MRLBM_ERR_INVALID_ARG, "too many boundary nodes");
+    }
+    h->n_list_pop = (int)list_xyz.size();
+    list_xyz.insert(list_xyz.end(), solid_xyz.begin(), solid_xyz.end());
+    list_word.insert(list_word.end(), solid_word.begin(), solid_word.end());
+    h->n_list = (int)list_xyz.size();
+    h->n_list_blocks = special_list_blocks(h->n_list);
     const int nseg = (d.nz + h->lz - 1) / h->lz;
     std::vector<int32_t> items;
     for (int s = 0; s < nseg; ++s)
@@ -394,7 +445,13 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     CK(H, cudaMemset(h->d_error, 0, sizeof(int)));
     CK(H, cudaMalloc((void **)&h->d_force_ring, (size_t)kRing * 10 * sizeof(double)));
     CK(H, cudaMalloc((void **)&h->d_diag_ring, (size_t)kRing * 2 * sizeof(double)));
-    CK(H, cudaMalloc((void **)&h->d_diag_part, (size_t)h->n_ctas * 2 * sizeof(double)));
+    CK(H, cudaMalloc((void **)&h->d_diag_part, (size_t)(h->n_ctas + h->n_list_blocks) * 2 * sizeof(double)));
+    if (h->n_list > 0) {
+        CK(H, upload(&h->d_list_xyz, list_xyz.data(), list_xyz.size()));
+        CK(H, upload(&h->d_list_word, list_word.data(), list_word.size()));
+        CK(H, upload(&h->d_row_base, row_base.data(), row_base.size()));
+        if (h->n_list_pop > 0) CK(H, cudaMalloc((void **)&h->d_popbuf, (size_t)h->n_list_pop * 27 * sizeof(float)));
+    }
     h->force_steps.assign(kRing, -1);
     h->diag_steps.assign(kRing, -1);
 
@@ -407,6 +464,12 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     a.n_items = h->n_items;
     a.tile_slot = h->d_tile_slot;
     a.side = h->d_side;
+    a.list_xyz = h->d_list_xyz;
+    a.list_word = h->d_list_word;
+    a.n_list_pop = h->n_list_pop;
+    a.n_list = h->n_list;
+    a.popbuf = h->d_popbuf;
+    a.row_base = h->d_row_base;
     a.nx = d.nx;
     a.ny = d.ny;
     a.nz = d.nz;
@@ -550,10 +613,14 @@ int mrlbm_step(mrlbm_handle *h, int32_t nsteps) {
         }
         if (ds) L.diag_part = h->d_diag_part;
         CK(h, launch_step(L, h->storage, h->tile_y, h->d_word != nullptr, h->stream));
+        if (h->n_list > 0)
+            CK(h, launch_special_list(L, h->storage, h->n_list_blocks, ds ? h->d_diag_part + 2 * h->n_ctas : nullptr,
+                                      h->stream));
         if (nb > 0) CK(h, launch_wall(L, h->storage, nb + (fs ? nbf : 0), h->stream));
         if (ds) {
             const int64_t slot = h->diag_count % kRing;
-            CK(h, launch_diag_finalize(h->d_diag_part, h->n_ctas, h->d_diag_ring + slot * 2, h->stream));
+            CK(h, launch_diag_finalize(h->d_diag_part, h->n_ctas + (h->n_list > 0 ? h->n_list_blocks : 0),
+                                       h->d_diag_ring + slot * 2, h->stream));
             h->diag_steps[slot] = it;
             ++h->diag_count;
         }

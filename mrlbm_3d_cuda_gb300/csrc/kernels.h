@@ -54,6 +54,14 @@ struct StepArgs {
     WallArgs wall[2];
     const uint32_t *tag_in = nullptr, *tag_out = nullptr;  // [256] BCFLUID masks
     int *error = nullptr;     // sticky device error flag
+    // non-bulk node list (special tiles only): entries [0, n_list_pop) get their 27 pulled
+    // populations from the step kernel, in (tile slot, z, tile row, x) order; entries
+    // [n_list_pop, n_list) are solid nodes of updated blocks (no populations)
+    const uint64_t *list_xyz = nullptr;   // x | y << 21 | z << 42
+    const uint32_t *list_word = nullptr;  // node word of each entry
+    int n_list_pop = 0, n_list = 0;
+    float *popbuf = nullptr;              // [27][n_list_pop]
+    const int32_t *row_base = nullptr;    // [slot][z][tile row]: first list entry of the row
 };
 
 // Per-step launch parameters.
@@ -77,6 +85,9 @@ int step_kernel_smem_bytes(int tile_y);
 int step_kernel_max_ctas_per_sm(int storage, int tile_y);
 // Curved-wall closure + collision for the wall nodes of both walls, plus the force sums.
 cudaError_t launch_wall(const StepLaunch &l, int storage, int n_total, cudaStream_t s);
+// Closures, stencil snapshots and collision of the listed non-bulk nodes (after launch_step).
+int special_list_blocks(int n_list);
+cudaError_t launch_special_list(const StepLaunch &l, int storage, int n_blocks, double *diag_part, cudaStream_t s);
 // Sum the per-CTA diagnostics partials into out[2] in a fixed order.
 cudaError_t launch_diag_finalize(const double *part, int n, double *out, cudaStream_t s);
 

@@ -1,0 +1,171 @@
+// Boundary and other non-bulk nodes: one thread per listed node, after the step kernel.
+//
+// The step kernel updates every plain bulk node in its fused pass.  For a node that carries a
+// node word (domain faces / edges / corners, BCFLUID, curved-wall nodes, wall-stencil nodes)
+// it only exports the 27 pulled populations to a list-ordered buffer; this kernel applies the
+// node's closure, snapshots stencil nodes for the wall kernel, collides and stores.  Solid
+// nodes of updated blocks get no populations: the reference only collides their stored
+// moments.  Nodes of blocks the reference never updates (frozen) are in no list.
+//
+// Reference (paths inside sakthi-lbm/MRLBM_3D_CUDA):
+//   evaluate_bounday_moments dispatch   MRLBM_3D/src/solver/mlbm.cu:166-184
+//   cylinder_boundary_moments / annulus_boundary_moments
+//                                       MRLBM_3D/src/cases/cylinder/cylinder_kernels.cuh:32-65,
+//                                       MRLBM_3D/src/cases/annulus/annulus_kernels.cuh:17-58
+//   boundary_condition (faces, edges, corners), fluid_boundary_condition (BCFLUID)
+//                                       MRLBM_3D/src/cases/cylinder/boundaries.cuh:8-1037
+//   evaluate_incoming_moments_rotated   MRLBM_3D/src/boundary/curvedLBM.cu:5-59
+//   moment_collision                    MRLBM_3D/src/solver/mlbm.cu:3-16
+//   compute_force_mass_kernel (BCFLUID part)  MRLBM_3D/src/statistics/forces.cu:25-133
+#include "mrlbm_internal.h"
+#include "storage.cuh"
+
+namespace mrlbm {
+namespace {
+
+// Closure of one listed node from its pulled populations `fl`.  Returns 0 when the node is
+// not stored here (wall nodes: the wall kernel finishes them), 1 to store the collided moments
+// `m`, 2 to store them and count the node in the fluid diagnostics.
+template <typename S>
+__device__ __forceinline__ int special_node(const StepArgs &a, int parity, bool force, uint32_t w, const float *fl,
+                                            int x, int y, int z, int slot, int x0, int y0, Mom &m) {
+    const uint32_t cls = w & NW_CLASS_MASK;
+    const S *__restrict__ src = (const S *)a.m[parity];
+    bool wall_node = false;
+    bool fluid = true;
+    if (cls == C_BULK) {
+        evaluate(fl, m);
+    } else {
+        const Mom prev = load_mom<S>(src, aos_index(x, y, z, a.nxb, a.ny), a.rho0, a.sc);
+        m = prev;  // nodes without a closure keep their pre-stream moments
+        if (cls == C_SOLID) {
+            fluid = false;
+        } else if (cls == C_INNER || cls == C_OUTER) {
+            const int wi = cls == C_INNER ? 0 : 1;
+            const uint32_t bi = w >> NW_PAYLOAD_SHIFT;
+            incoming_rotated(a.wall[wi].nx[bi], a.wall[wi].ny[bi], a.wall[wi].in_mask[bi], fl, m);
+            wall_node = true;
+            fluid = false;
+        } else if (cls == C_BCFLUID_INNER || cls == C_BCFLUID_OUTER) {
+            const uint32_t tag = (w >> NW_PAYLOAD_SHIFT) & 0xFFu;
+            Mom o = prev;
+            if (bcfluid_closure(tag, a.tag_in[tag], fl, a.bcf_strong, a.omega, o)) m = o;
+        } else {
+            PlanarCtx c;
+            c.omega = a.omega;
+            c.u_max = a.u_max;
+            c.rho0 = a.rho0;
+            c.convective = a.convective;
+            c.self_prev = prev;
+            if (class_walls(cls) & 2u) c.west_prev = load_mom<S>(src, aos_index(x - 1, y, z, a.nxb, a.ny), a.rho0, a.sc);
+            else c.west_prev = prev;
+            Mom o = prev;
+            if (planar_closure(cls, fl, c, o)) m = o;
+        }
+    }
+    if ((w & NW_STENCIL) && slot >= 0) {
+        float *e = a.side + side_index(slot, x, y, z, x0, y0, a.nz, TILE_X, a.tile_y) * 16;
+        e[0] = m.rho - a.rho0;
+        e[1] = m.ux; e[2] = m.uy; e[3] = m.uz;
+        e[4] = m.mxx; e[5] = m.myy; e[6] = m.mzz;
+        e[7] = m.mxy; e[8] = m.mxz; e[9] = m.myz;
+    }
+    if (wall_node) return 0;
+    const bool bcf = force && slot >= 0 && (cls == C_BCFLUID_INNER || cls == C_BCFLUID_OUTER);
+    double fin[4] = {0.0, 0.0, 0.0, 0.0};
+    const uint32_t tag = (w >> NW_PAYLOAD_SHIFT) & 0xFFu;
+    if (bcf) masked_momentum64(a.tag_in[tag], m, fin);
+    collide(m, a.omega);
+    if (bcf) {
+        double fo[4];
+        masked_momentum64(a.tag_out[tag], m, fo);
+        float *e = a.side + side_index(slot, x, y, z, x0, y0, a.nz, TILE_X, a.tile_y) * 16;
+        e[10] = (float)(fin[0] - fo[0]);
+        e[11] = (float)(fin[1] - fo[1]);
+        e[12] = (float)(fin[2] - fo[2]);
+        e[13] = (float)(fin[3] - fo[3]);
+    }
+    return fluid ? 2 : 1;
+}
+
+constexpr int kListThreads = 256;
+
+template <typename S>
+__global__ void __launch_bounds__(kListThreads) special_list_kernel(const StepArgs *__restrict__ ga, int parity,
+                                                                      int force, double *__restrict__ diag_part) {
+    const StepArgs &a = *ga;
+    S *__restrict__ dst = (S *)a.m[parity ^ 1];
+    const int n_pop = a.n_list_pop, n_all = a.n_list;
+    double dm = 0.0, de = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_all; i += gridDim.x * blockDim.x) {
+        const uint64_t p = a.list_xyz[i];
+        const int x = (int)(p & 0x1FFFFFu), y = (int)((p >> 21) & 0x1FFFFFu), z = (int)(p >> 42);
+        const uint32_t w = a.list_word[i];
+        float f[27];
+        if (i < n_pop) {
+#pragma unroll
+            for (int q = 0; q < 27; ++q) f[q] = a.popbuf[(int64_t)q * n_pop + i];
+        } else {
+#pragma unroll
+            for (int q = 0; q < 27; ++q) f[q] = 0.f;  // solid nodes use no populations
+        }
+        const int tx = x / TILE_X, ty = y / a.tile_y;
+        const int slot = a.tile_slot[ty * a.tiles_x + tx];
+        Mom m;
+        const int code = special_node<S>(a, parity, force != 0, w, f, x, y, z, slot, tx * TILE_X, ty * a.tile_y, m);
+        if (code) store_mom<S>(dst, aos_index(x, y, z, a.nxb, a.ny), m, a.rho0, a.sc);
+        if (code == 2 && diag_part) {
+            dm += (double)(m.rho - a.rho0);
+            de += 0.5 * (double)(m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
+        }
+    }
+    if (diag_part) {
+        // fixed-order block reduction -> diag_part[blockIdx.x]
+        __shared__ double red[2][kListThreads / 32];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            dm += __shfl_down_sync(0xffffffffu, dm, o);
+            de += __shfl_down_sync(0xffffffffu, de, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            red[0][threadIdx.x >> 5] = dm;
+            red[1][threadIdx.x >> 5] = de;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s0 = 0.0, s1 = 0.0;
+            for (int k = 0; k < kListThreads / 32; ++k) {
+                s0 += red[0][k];
+                s1 += red[1][k];
+            }
+            diag_part[2 * blockIdx.x + 0] = s0;
+            diag_part[2 * blockIdx.x + 1] = s1;
+        }
+    }
+}
+
+}  // namespace
+
+int special_list_blocks(int n_list) {
+    const int b = (n_list + kListThreads - 1) / kListThreads;
+    return b < 1 ? 1 : (b > 2048 ? 2048 : b);
+}
+
+cudaError_t launch_special_list(const StepLaunch &l, int storage, int n_blocks, double *diag_part, cudaStream_t s) {
+    switch (storage) {
+        case MRLBM_STORAGE_F32:
+            special_list_kernel<float><<<n_blocks, kListThreads, 0, s>>>(l.ga, l.parity, l.force != nullptr, diag_part);
+            break;
+        case MRLBM_STORAGE_F16:
+            special_list_kernel<__half><<<n_blocks, kListThreads, 0, s>>>(l.ga, l.parity, l.force != nullptr, diag_part);
+            break;
+        case MRLBM_STORAGE_BF16:
+            special_list_kernel<__nv_bfloat16>
+                <<<n_blocks, kListThreads, 0, s>>>(l.ga, l.parity, l.force != nullptr, diag_part);
+            break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace mrlbm

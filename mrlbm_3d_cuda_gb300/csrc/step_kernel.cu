@@ -77,76 +77,6 @@ __device__ __forceinline__ void rim_store(const Mom &m, float *up, float *fl, fl
     }
 }
 
-// Non-bulk node: boundary closure, stencil snapshot, BCFLUID force.  Works on a private
-// copy of the pulled populations so the bulk path keeps its registers.  Returns 0 when the
-// node is not stored here, 1 to store the collided moments `m`, 2 to store them and count
-// the node in the fluid diagnostics.
-template <typename S, int TY>
-__device__ __noinline__ int special_node(const StepArgs *__restrict__ ga, int parity, bool force, uint32_t w,
-                                         float *fl, int x, int y, int z, int64_t node, int slot, int x0, int y0,
-                                         Mom &m) {
-    if (w & NW_FROZEN) return 0;  // block the reference never updates
-    const StepArgs &a = *ga;
-    const uint32_t cls = w & NW_CLASS_MASK;
-    const S *__restrict__ src = (const S *)a.m[parity];
-    bool wall_node = false;
-    bool fluid = true;
-    if (cls == C_BULK) {
-        evaluate(fl, m);
-    } else {
-        const Mom prev = load_mom<S>(src, aos_index(x, y, z, a.nxb, a.ny), a.rho0, a.sc);
-        m = prev;  // nodes without a closure keep their pre-stream moments
-        if (cls == C_SOLID) {
-            fluid = false;
-        } else if (cls == C_INNER || cls == C_OUTER) {
-            const int wi = cls == C_INNER ? 0 : 1;
-            const uint32_t bi = w >> NW_PAYLOAD_SHIFT;
-            incoming_rotated(a.wall[wi].nx[bi], a.wall[wi].ny[bi], a.wall[wi].in_mask[bi], fl, m);
-            wall_node = true;
-            fluid = false;
-        } else if (cls == C_BCFLUID_INNER || cls == C_BCFLUID_OUTER) {
-            const uint32_t tag = (w >> NW_PAYLOAD_SHIFT) & 0xFFu;
-            Mom o = prev;
-            if (bcfluid_closure(tag, a.tag_in[tag], fl, a.bcf_strong, a.omega, o)) m = o;
-        } else {
-            PlanarCtx c;
-            c.omega = a.omega;
-            c.u_max = a.u_max;
-            c.rho0 = a.rho0;
-            c.convective = a.convective;
-            c.self_prev = prev;
-            if (class_walls(cls) & 2u) c.west_prev = load_mom<S>(src, aos_index(x - 1, y, z, a.nxb, a.ny), a.rho0, a.sc);
-            else c.west_prev = prev;
-            Mom o = prev;
-            if (planar_closure(cls, fl, c, o)) m = o;
-        }
-    }
-    if ((w & NW_STENCIL) && slot >= 0) {
-        float *e = a.side + side_index(slot, x, y, z, x0, y0, a.nz, TILE_X, TY) * 16;
-        e[0] = m.rho - a.rho0;
-        e[1] = m.ux; e[2] = m.uy; e[3] = m.uz;
-        e[4] = m.mxx; e[5] = m.myy; e[6] = m.mzz;
-        e[7] = m.mxy; e[8] = m.mxz; e[9] = m.myz;
-    }
-    if (wall_node) return 0;  // the wall kernel finishes this node
-    const bool bcf = force && slot >= 0 && (cls == C_BCFLUID_INNER || cls == C_BCFLUID_OUTER);
-    double fin[4] = {0.0, 0.0, 0.0, 0.0};
-    const uint32_t tag = (w >> NW_PAYLOAD_SHIFT) & 0xFFu;
-    if (bcf) masked_momentum64(a.tag_in[tag], m, fin);
-    collide(m, a.omega);
-    if (bcf) {
-        double fo[4];
-        masked_momentum64(a.tag_out[tag], m, fo);
-        float *e = a.side + side_index(slot, x, y, z, x0, y0, a.nz, TILE_X, TY) * 16;
-        e[10] = (float)(fin[0] - fo[0]);
-        e[11] = (float)(fin[1] - fo[1]);
-        e[12] = (float)(fin[2] - fo[2]);
-        e[13] = (float)(fin[3] - fo[3]);
-    }
-    return fluid ? 2 : 1;
-}
-
-
 // Pulled population q of the owner node, read from the ring buffer of its c_z class.
 template <int Q, int TY>
 __device__ __forceinline__ float pull(const float *up, const float *fl, const float *dn, int col) {
@@ -297,6 +227,10 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     const int32_t *__restrict__ items = ga->items;
     const int32_t *__restrict__ tile_slot = ga->tile_slot;
     const uint32_t *__restrict__ word = ga->word;
+    float *__restrict__ popbuf = ga->popbuf;
+    const int n_pop = ga->n_list_pop;
+    const int32_t *__restrict__ row_base = ga->row_base;
+    (void)force;  // boundary forces are integrated by the node-list and wall kernels
     const float omega = ga->omega, rho0 = ga->rho0;
     const StorageScale sc = ga->sc;
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
@@ -364,10 +298,24 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
             float c0 = 0.f, c5 = 0.f, c6 = 0.f;   // own-column rest / up / down populations of plane k
             float p0 = 0.f, p5 = 0.f, pp5 = 0.f;  // f0(k-1), f5(k-1), f5(k-2)
             float dm = 0.f, de = 0.f;
-            auto owner_plane = [&](const int k, const float (&cur)[10], float (&nxt)[10]) {
+            // special tiles: node word and list row base of the plane emitted two planes later,
+            // one queue slot per plane parity
+            uint32_t wqa = 0u, wqb = 0u;
+            int rqa = 0, rqb = 0;
+            const unsigned row_mask = w >= 32 ? 0xffffffffu : ((1u << w) - 1u);
+            auto owner_plane = [&](const int k, const float (&cur)[10], float (&nxt)[10], uint32_t &wq, int &rq) {
                 float *up = up_base + k4 * G::PLANE;
                 float *flt = fl_base + k3 * G::PLANE;
                 float *dn = dn_base + (k & 1) * G::PLANE;
+                uint32_t wnew = 0u;
+                int rnew = 0;
+                if constexpr (SPECIAL) {
+                    if (slot >= 0 && own && k + 2 <= last) {
+                        const int zq = zs + k;
+                        wnew = word[(int64_t)x + (int64_t)nx * y + (int64_t)zq * plane];
+                        rnew = row_base[((int64_t)slot * nz + zq) * TY + ty];
+                    }
+                }
                 if (own) {
                     if (k < last) {
                         load_raw<S>(src, cxy + (int64_t)zn * zst, nxt);
@@ -382,8 +330,16 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                         const float *eup = up_base + (k4 >= 2 ? k4 - 2 : k4 + 2) * G::PLANE;  // plane k-2
                         const float *efl = fl_base + (k3 >= 1 ? k3 - 1 : 2) * G::PLANE;       // plane k-1
                         const int64_t ai = cxy + (int64_t)z * zst;
-                        const int64_t node = (int64_t)x + (int64_t)nx * y + (int64_t)z * plane;
-                        const uint32_t wd = (SPECIAL && slot >= 0) ? word[node] : 0u;
+                        uint32_t wd = 0u;
+                        bool exp = false;
+                        unsigned bal = 0u;
+                        if constexpr (SPECIAL) {
+                            if (slot >= 0) {
+                                wd = wq;
+                                exp = wd != 0u && !(wd & NW_FROZEN) && (wd & NW_CLASS_MASK) != C_SOLID;
+                                bal = __ballot_sync(row_mask, exp);
+                            }
+                        }
                         if (wd == 0u) {
                             Mom m;
                             gather_evaluate<TY>(eup, efl, dn, col, p0, pp5, c6, m);
@@ -393,21 +349,19 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                             }
                             collide(m, omega);
                             store_mom<S>(dst, ai, m, rho0, sc);
-                        } else if constexpr (SPECIAL) {
+                        } else if (exp) {
+                            // non-bulk node: hand its pulled populations to the node-list kernel
                             float fw[27];
                             gather_all<TY>(eup, efl, dn, col, p0, pp5, c6, fw);
-                            Mom ms;
-                            const int code = special_node<S, TY>(ga, parity, force != nullptr, wd, fw, x, y, z, node,
-                                                                 slot, x0, y0, ms);
-                            if (code) store_mom<S>(dst, ai, ms, rho0, sc);
-                            if (code == 2 && diag) {
-                                dm += ms.rho - rho0;
-                                de += 0.5f * (ms.ux * ms.ux + ms.uy * ms.uy + ms.uz * ms.uz);
-                            }
+                            float *pq = popbuf + (rq + __popc(bal & ((1u << tx) - 1u)));
+#pragma unroll
+                            for (int q = 0; q < 27; ++q) pq[(int64_t)q * n_pop] = fw[q];
                         }
                     }
                     if (k + 2 <= last) nb_arrive(3 + (k & 1), G::NTH);  // DONE(k)
                 }
+                wq = wnew;
+                rq = rnew;
                 pp5 = p5;
                 p5 = c5;
                 p0 = c0;
@@ -415,8 +369,8 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 k4 = (k4 + 1) & 3;
             };
             for (int k = 0; k <= last; k += 2) {
-                owner_plane(k, pa, pb);
-                if (k + 1 <= last) owner_plane(k + 1, pb, pa);
+                owner_plane(k, pa, pb, wqa, rqa);
+                if (k + 1 <= last) owner_plane(k + 1, pb, pa, wqb, rqb);
             }
             if (diag) {
                 dmD += (double)dm;
