@@ -145,6 +145,7 @@ typedef struct mrlbm_info {
 } mrlbm_info;
 
 typedef struct mrlbm_handle mrlbm_handle;
+typedef struct mrlbm_batch mrlbm_batch;
 
 /* ---- lifecycle ------------------------------------------------------------------------- */
 int mrlbm_abi_version(void);
@@ -212,6 +213,33 @@ int mrlbm_write_vti(mrlbm_handle *h, const char *path);       /* data<10000000+i
  * asynchronous on `cuda_stream` (a cudaStream_t; NULL = default stream). */
 int mrlbm_step_periodic_noalloc(const float *m_in, float *m_out, int32_t nx, int32_t ny, int32_t nz, float omega,
                                 float rho0, double *diag, void *cuda_stream);
+
+/* ---- autotuning and batches (no counterpart in the reference: its tile shape is a
+ * compile-time constant and it runs one case per process) ----------------------------------- */
+/* Time every tile height (4, 8, 16) with every z-segment length (the built-in heuristic and
+ * powers of two below nz) over `trial_steps` steps and keep the fastest.  The moments, step
+ * counter and sampling state are restored afterwards; results do not depend on the tiling.
+ * tile_out (optional): {32, tile height, z-segment length}. */
+int mrlbm_autotune(mrlbm_handle *h, int32_t trial_steps, int32_t tile_out[3]);
+/* Several independent cases (uneven grids allowed; one moment storage for all) advanced
+ * together: per step one persistent step-kernel launch over the work items of every case,
+ * one node-list launch and one wall launch, replayed from CUDA graphs.  Proposed in place of
+ * running the reference once per case (MRLBM_3D/src/main.cu:7-40). */
+int mrlbm_batch_create(const mrlbm_case_desc *descs, int32_t n, mrlbm_batch **out);
+int mrlbm_batch_destroy(mrlbm_batch *b);
+int mrlbm_batch_size(const mrlbm_batch *b);
+/* Handle of case i, for init / set / get moments, forces and info.  It runs on the batch's
+ * stream; mrlbm_step, mrlbm_destroy, mrlbm_set_stream and mrlbm_autotune on it return
+ * MRLBM_ERR_STATE. */
+int mrlbm_batch_handle(mrlbm_batch *b, int32_t i, mrlbm_handle **h);
+/* Force sampling period for every case (0 = off); batches keep no mass / energy samples. */
+int mrlbm_batch_set_sampling(mrlbm_batch *b, int32_t force_every);
+int mrlbm_batch_step(mrlbm_batch *b, int32_t nsteps);
+/* The same steps as plain per-case launches, case after case (the unbatched comparison). */
+int mrlbm_batch_step_sequential(mrlbm_batch *b, int32_t nsteps);
+/* Batch-wide tile height and z-segment cap, timed like mrlbm_autotune. */
+int mrlbm_batch_autotune(mrlbm_batch *b, int32_t trial_steps, int32_t tile_out[3]);
+int mrlbm_batch_sync(mrlbm_batch *b);
 
 #ifdef __cplusplus
 }

@@ -10,7 +10,7 @@ this package builds it in-tree and binds it with ctypes:
 """
 from . import native
 from .native import MrlbmError
-from .simulation import Case, Simulation
+from .simulation import Batch, Case, Simulation
 from . import cases
 
-__all__ = ["native", "MrlbmError", "Case", "Simulation", "cases"]
+__all__ = ["native", "MrlbmError", "Batch", "Case", "Simulation", "cases"]

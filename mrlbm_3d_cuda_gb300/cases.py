@@ -114,6 +114,27 @@ def c3_annulus(storage: int = N.STORAGE_F32) -> N.CaseDesc:
     return annulus(160, 160, 128, 32.0, 64.0, 0.05, 400.0, storage=storage)
 
 
+def c4_batch(n: int = 64, seed: int = 1234, storage: int = N.STORAGE_F32) -> list:
+    """Independent cylinder-in-channel cases for batched stepping: per case D ~ U{8..40} and
+    Re ~ U[20, 300) drawn in that order from numpy's default generator (PCG64) seeded with
+    `seed`; Lx = 12D, Ly = 6D rounded up to multiples of 8 (<= 512 / 256), Lz = 3D rounded up
+    to a multiple of 4 (<= 64), centre (4D, 3D), inlet u = 0.05, zero-gradient outlet,
+    no-slip y walls, periodic z."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+
+    def up(v, m):
+        return ((v + m - 1) // m) * m
+
+    for _ in range(n):
+        d = int(rng.integers(8, 41))
+        re = float(rng.uniform(20.0, 300.0))
+        lx, ly, lz = min(up(12 * d, 8), 512), min(up(6 * d, 8), 256), min(up(3 * d, 4), 64)
+        out.append(cylinder_channel(lx, ly, lz, d, 4.0 * d, 3.0 * d, 0.05, re, storage=storage))
+    return out
+
+
 def c5_turbulent_cylinder(storage: int = N.STORAGE_F16) -> N.CaseDesc:
     """Large cylinder: 1024 x 512 x 256, D = 64 at (256, 256), Re = 3900, U = 0.05."""
     return cylinder_channel(1024, 512, 256, 64, 256.0, 256.0, 0.05, 3900.0, storage=storage)

@@ -10,6 +10,7 @@
 #include <fstream>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -60,6 +61,8 @@ struct mrlbm_handle {
     uint32_t *d_tag = nullptr;  // [512]: in masks then out masks
     StepArgs args{};
     StepArgs *d_args = nullptr;
+    std::vector<int32_t> h_items;   // host copy of the work items
+    mrlbm_batch *batch = nullptr;   // owning batch, if any
     int *d_error = nullptr;
     // sampling
     int force_every = 0, diag_every = 0;
@@ -69,6 +72,28 @@ struct mrlbm_handle {
     // staging
     float *d_stage = nullptr;
     size_t stage_bytes = 0;
+};
+
+// Independent cases advanced together: every step is one persistent step-kernel launch over
+// the work items of all cases, one node-list launch and one wall launch, replayed from CUDA
+// graphs (one per ping-pong parity and force sampling).
+struct mrlbm_batch {
+    std::vector<mrlbm_handle *> h;
+    cudaStream_t stream = nullptr;
+    int storage = 0, tile_y = 16, lz = 0;
+    int parity = 0;
+    int64_t step = 0;
+    int force_every = 0;
+    int64_t force_count = 0;  // sampled steps so far (the ring slot of the cases with walls)
+    // device tables (BatchArgs and what it points to)
+    const StepArgs **d_cases = nullptr;
+    int2 *d_items = nullptr;
+    int4 *d_list_blocks = nullptr, *d_wall_blocks = nullptr;
+    double **d_ring = nullptr;
+    int *d_slot = nullptr;
+    BatchArgs *d_ba = nullptr;
+    int n_items = 0, n_ctas = 0, n_list_blocks = 0, n_wall_blocks = 0;
+    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [parity][force]
 };
 
 namespace {
@@ -149,29 +174,232 @@ int ensure_stage(mrlbm_handle *h, size_t bytes) {
     return MRLBM_OK;
 }
 
-int choose_tiling(mrlbm_handle *h) {
+// Tile height and z-segment length from MRLBM_TILE_Y / MRLBM_LZ, else the defaults: 32 x 16
+// columns (the widest tile amortises the rim rebuild best: at 256^3 FP32 on GB300, 32 x 16 /
+// 32 x 8 / 32 x 4 run at 0.36 / 0.42 / 0.47 ms per step) and lz = 0, the heuristic below.
+void default_tiling(int &ty, int &lz) {
     const char *ety = std::getenv("MRLBM_TILE_Y");
     const char *elz = std::getenv("MRLBM_LZ");
-    // 32 x 16 columns by default: the widest tile amortises the rim rebuild best (at 256^3
-    // FP32 on GB300: 32 x 16 / 32 x 8 / 32 x 4 run at 0.36 / 0.42 / 0.47 ms per step)
-    int ty = ety ? std::atoi(ety) : 16;
+    ty = ety ? std::atoi(ety) : 16;
     if (ty != 4 && ty != 8 && ty != 16) ty = 16;
+    lz = elz ? std::max(1, std::atoi(elz)) : 0;
+}
+
+int setup_tiling(mrlbm_handle *h, int ty, int lz);
+
+// (Re)build everything that depends on the step kernel's tiling: tile slots and side buffer,
+// the non-bulk node list, work items, grid size and the device StepArgs.  Node words and
+// geometry do not depend on it, so the autotuner can switch tilings cheaply.
+int setup_tiling(mrlbm_handle *h, int ty, int lz) {
+    const mrlbm_case_desc &d = h->d;
+    const Geometry &g = h->geo;
+    if (ty != 4 && ty != 8 && ty != 16) return fail(h, MRLBM_ERR_INVALID_ARG, "tile height must be 4, 8 or 16");
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (void **p : {(void **)&h->d_tile_slot, (void **)&h->d_side, (void **)&h->d_items, (void **)&h->d_list_xyz,
+                     (void **)&h->d_list_word, (void **)&h->d_row_base, (void **)&h->d_popbuf,
+                     (void **)&h->d_diag_part}) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
     h->tile_y = ty;
-    h->tiles_x = (h->d.nx + TILE_X - 1) / TILE_X;
-    h->tiles_y = (h->d.ny + ty - 1) / ty;
+    h->tiles_x = (d.nx + TILE_X - 1) / TILE_X;
+    h->tiles_y = (d.ny + ty - 1) / ty;
     int per_sm = step_kernel_max_ctas_per_sm(h->storage, ty);
     if (per_sm <= 0) per_sm = 1;
     const int resident = per_sm * h->n_sm;
     const int tiles = h->tiles_x * h->tiles_y;
-    int lz = h->d.nz;
-    if (elz) {
-        lz = std::max(1, std::min(h->d.nz, std::atoi(elz)));
+    if (lz > 0) {
+        lz = std::min(d.nz, lz);
     } else {
         // longest z-segment that still gives every resident CTA several work items
-        while (lz > 16 && (int64_t)tiles * ((h->d.nz + lz - 1) / lz) < 4LL * resident) lz = (lz + 1) / 2;
+        lz = d.nz;
+        while (lz > 16 && (int64_t)tiles * ((d.nz + lz - 1) / lz) < 4LL * resident) lz = (lz + 1) / 2;
     }
     h->lz = lz;
-    return resident;
+    std::vector<uint32_t> word(h->n, 0);
+    for (int64_t i = 0; i < h->n; ++i) word[i] = make_word(g.cls[i], g.payload[i], g.frozen[i] != 0, g.stencil[i] != 0);
+    std::vector<int32_t> slot(tiles, -1);
+    std::vector<char> skip(tiles, 0);
+    int n_special = 0;
+    for (int t = 0; t < tiles; ++t) {
+        const int x0 = (t % h->tiles_x) * TILE_X, y0 = (t / h->tiles_x) * h->tile_y;
+        bool special = false, all_frozen = true;
+        for (int z = 0; z < d.nz; ++z)
+            for (int y = y0; y < std::min(d.ny, y0 + h->tile_y); ++y)
+                for (int x = x0; x < std::min(d.nx, x0 + TILE_X); ++x) {
+                    const int64_t i = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
+                    if (word[i]) special = true;
+                    if (!g.frozen[i]) all_frozen = false;
+                }
+        if (all_frozen) skip[t] = 1;
+        else if (special) slot[t] = n_special++;
+    }
+    h->n_special = n_special;
+
+    // Non-bulk nodes of special tiles, in the order the step kernel exports their pulled
+    // populations: slot, z, tile row, x.  Solid nodes of updated blocks need no populations
+    // and follow the others; frozen nodes are never updated and are in no list.
+    std::vector<uint64_t> list_xyz;
+    std::vector<uint32_t> list_word;
+    std::vector<int32_t> row_base((size_t)n_special * d.nz * h->tile_y, 0);
+    std::vector<uint64_t> solid_xyz;
+    std::vector<uint32_t> solid_word;
+    for (int t = 0; t < tiles; ++t) {
+        if (slot[t] < 0) continue;
+        const int x0 = (t % h->tiles_x) * TILE_X, y0 = (t / h->tiles_x) * h->tile_y;
+        for (int z = 0; z < d.nz; ++z)
+            for (int r = 0; r < h->tile_y; ++r) {
+                row_base[((size_t)slot[t] * d.nz + z) * h->tile_y + r] = (int32_t)list_xyz.size();
+                const int y = y0 + r;
+                if (y >= d.ny) continue;
+                for (int x = x0; x < std::min(d.nx, x0 + TILE_X); ++x) {
+                    const int64_t i = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
+                    const uint32_t wd = word[i];
+                    if (wd == 0u || (wd & NW_FROZEN)) continue;
+                    const uint64_t p = (uint64_t)x | ((uint64_t)y << 21) | ((uint64_t)z << 42);
+                    if ((wd & NW_CLASS_MASK) == C_SOLID) {
+                        solid_xyz.push_back(p);
+                        solid_word.push_back(wd);
+                    } else {
+                        list_xyz.push_back(p);
+                        list_word.push_back(wd);
+                    }
+                }
+            }
+    }
+    if (list_xyz.size() + solid_xyz.size() >= (size_t)INT32_MAX / 27)
+        return fail(h, MRLBM_ERR_INVALID_ARG, "too many boundary nodes");
+    h->n_list_pop = (int)list_xyz.size();
+    list_xyz.insert(list_xyz.end(), solid_xyz.begin(), solid_xyz.end());
+    list_word.insert(list_word.end(), solid_word.begin(), solid_word.end());
+    h->n_list = (int)list_xyz.size();
+    h->n_list_blocks = special_list_blocks(h->n_list);
+    const int nseg = (d.nz + h->lz - 1) / h->lz;
+    std::vector<int32_t> items;
+    for (int s = 0; s < nseg; ++s)
+        for (int t = 0; t < tiles; ++t)
+            if (!skip[t]) items.push_back(t | (s << 20));
+    h->n_items = (int)items.size();
+    h->n_ctas = std::max(1, std::min(h->n_items, resident));
+    h->h_items = items;
+
+    if (h->d_word) {
+        CK(h, upload(&h->d_tile_slot, slot.data(), slot.size()));
+        if (n_special > 0) {
+            const size_t side_floats = (size_t)n_special * d.nz * TILE_X * h->tile_y * 16;
+            CK(h, cudaMalloc((void **)&h->d_side, side_floats * sizeof(float)));
+            CK(h, cudaMemset(h->d_side, 0, side_floats * sizeof(float)));
+        }
+    }
+    CK(h, upload(&h->d_items, items.data(), items.size()));
+    CK(h, cudaMalloc((void **)&h->d_diag_part, (size_t)(h->n_ctas + h->n_list_blocks) * 2 * sizeof(double)));
+    if (h->n_list > 0) {
+        CK(h, upload(&h->d_list_xyz, list_xyz.data(), list_xyz.size()));
+        CK(h, upload(&h->d_list_word, list_word.data(), list_word.size()));
+        CK(h, upload(&h->d_row_base, row_base.data(), row_base.size()));
+        if (h->n_list_pop > 0) CK(h, cudaMalloc((void **)&h->d_popbuf, (size_t)h->n_list_pop * 27 * sizeof(float)));
+    }
+    StepArgs &a = h->args;
+    a.items = h->d_items;
+    a.n_items = h->n_items;
+    a.tile_slot = h->d_tile_slot;
+    a.side = h->d_side;
+    a.list_xyz = h->d_list_xyz;
+    a.list_word = h->d_list_word;
+    a.n_list_pop = h->n_list_pop;
+    a.n_list = h->n_list;
+    a.popbuf = h->d_popbuf;
+    a.row_base = h->d_row_base;
+    a.tiles_x = h->tiles_x;
+    a.tiles_y = h->tiles_y;
+    a.tile_y = h->tile_y;
+    a.lz = h->lz;
+    CK(h, cudaMemcpy(h->d_args, &a, sizeof(StepArgs), cudaMemcpyHostToDevice));
+    return MRLBM_OK;
+}
+
+// One or more time steps of one handle: step kernel, node-list kernel, wall kernel and the
+// sampled force / diagnostics reductions, all asynchronous on the handle's stream.
+int step_handle(mrlbm_handle *h, int32_t nsteps) {
+    const int nb = (int)(h->geo.wall[0].list.size() + h->geo.wall[1].list.size());
+    const int nbf = (int)(h->geo.wall[0].fluid_list.size() + h->geo.wall[1].fluid_list.size());
+    for (int s = 0; s < nsteps; ++s) {
+        const int64_t it = h->step;
+        const bool fs = h->force_every > 0 && it % h->force_every == 0;
+        const bool ds = h->diag_every > 0 && it % h->diag_every == 0;
+        StepLaunch L;
+        L.ga = h->d_args;
+        L.parity = h->parity;
+        L.n_ctas = h->n_ctas;
+        if (fs) {
+            const int64_t slot = h->force_count % kRing;
+            L.force = h->d_force_ring + slot * 10;
+            CK(h, cudaMemsetAsync(L.force, 0, 10 * sizeof(double), h->stream));
+            h->force_steps[slot] = it;
+            ++h->force_count;
+        }
+        if (ds) L.diag_part = h->d_diag_part;
+        CK(h, launch_step(L, h->storage, h->tile_y, h->d_word != nullptr, h->stream));
+        if (h->n_list > 0)
+            CK(h, launch_special_list(L, h->storage, h->n_list_blocks, ds ? h->d_diag_part + 2 * h->n_ctas : nullptr,
+                                      h->stream));
+        if (nb > 0) CK(h, launch_wall(L, h->storage, nb + (fs ? nbf : 0), h->stream));
+        if (ds) {
+            const int64_t slot = h->diag_count % kRing;
+            CK(h, launch_diag_finalize(h->d_diag_part, h->n_ctas + (h->n_list > 0 ? h->n_list_blocks : 0),
+                                       h->d_diag_ring + slot * 2, h->stream));
+            h->diag_steps[slot] = it;
+            ++h->diag_count;
+        }
+        h->parity ^= 1;
+        ++h->step;
+    }
+    return MRLBM_OK;
+}
+
+// Candidate z-segment lengths for the autotuner: 0 (the per-case heuristic) and powers of two
+// below nz.
+std::vector<int> lz_candidates(int nz) {
+    std::vector<int> v{0};
+    for (int lz = 8; lz < nz; lz *= 2) v.push_back(lz);
+    return v;
+}
+
+// Saved time-step state: the current moment buffer and the step / sampling counters, so the
+// autotuner's trial steps leave no trace.
+struct SavedState {
+    void *buf = nullptr;
+    int parity = 0, force_every = 0, diag_every = 0;
+    int64_t step = 0, force_count = 0, diag_count = 0;
+};
+
+int save_state(mrlbm_handle *h, SavedState &st) {
+    const size_t bytes = (size_t)h->fs * h->vbytes;
+    CK(h, cudaMalloc(&st.buf, bytes));
+    CK(h, cudaMemcpyAsync(st.buf, h->m[h->parity], bytes, cudaMemcpyDeviceToDevice, h->stream));
+    st.parity = h->parity;
+    st.force_every = h->force_every;
+    st.diag_every = h->diag_every;
+    st.step = h->step;
+    st.force_count = h->force_count;
+    st.diag_count = h->diag_count;
+    h->force_every = h->diag_every = 0;
+    return MRLBM_OK;
+}
+
+int restore_state(mrlbm_handle *h, SavedState &st) {
+    const size_t bytes = (size_t)h->fs * h->vbytes;
+    CK(h, cudaMemcpyAsync(h->m[st.parity], st.buf, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    cudaFree(st.buf);
+    st.buf = nullptr;
+    h->parity = st.parity;
+    h->force_every = st.force_every;
+    h->diag_every = st.diag_every;
+    h->step = st.step;
+    h->force_count = st.force_count;
+    h->diag_count = st.diag_count;
+    return MRLBM_OK;
 }
 
 }  // namespace
@@ -330,9 +558,7 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
         h->sc.is[k] = 1.0f / s;
     }
 
-    // node words, tile classes, work items
-    const int resident = choose_tiling(h.get());
-    const int tiles = h->tiles_x * h->tiles_y;
+    // node words (tile independent)
     std::vector<uint32_t> word(h->n, 0);
     bool any_special = false;
     int64_t n_fluid = 0;
@@ -343,71 +569,6 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
         if (!g.frozen[i] && c != C_SOLID && c != C_INNER && c != C_OUTER) ++n_fluid;
     }
     h->n_fluid = n_fluid;
-    std::vector<int32_t> slot(tiles, -1);
-    std::vector<char> skip(tiles, 0);
-    int n_special = 0;
-    for (int t = 0; t < tiles; ++t) {
-        const int x0 = (t % h->tiles_x) * TILE_X, y0 = (t / h->tiles_x) * h->tile_y;
-        bool special = false, all_frozen = true;
-        for (int z = 0; z < d.nz; ++z)
-            for (int y = y0; y < std::min(d.ny, y0 + h->tile_y); ++y)
-                for (int x = x0; x < std::min(d.nx, x0 + TILE_X); ++x) {
-                    const int64_t i = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
-                    if (word[i]) special = true;
-                    if (!g.frozen[i]) all_frozen = false;
-                }
-        if (all_frozen) skip[t] = 1;
-        else if (special) slot[t] = n_special++;
-    }
-    h->n_special = n_special;
-
-    // Non-bulk nodes of special tiles, in the order the step kernel exports their pulled
-    // populations: slot, z, tile row, x.  Solid nodes of updated blocks need no populations
-    // and follow the others; frozen nodes are never updated and are in no list.
-    std::vector<uint64_t> list_xyz;
-    std::vector<uint32_t> list_word;
-    std::vector<int32_t> row_base((size_t)n_special * d.nz * h->tile_y, 0);
-    std::vector<uint64_t> solid_xyz;
-    std::vector<uint32_t> solid_word;
-    for (int t = 0; t < tiles; ++t) {
-        if (slot[t] < 0) continue;
-        const int x0 = (t % h->tiles_x) * TILE_X, y0 = (t / h->tiles_x) * h->tile_y;
-        for (int z = 0; z < d.nz; ++z)
-            for (int r = 0; r < h->tile_y; ++r) {
-                row_base[((size_t)slot[t] * d.nz + z) * h->tile_y + r] = (int32_t)list_xyz.size();
-                const int y = y0 + r;
-                if (y >= d.ny) continue;
-                for (int x = x0; x < std::min(d.nx, x0 + TILE_X); ++x) {
-                    const int64_t i = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
-                    const uint32_t wd = word[i];
-                    if (wd == 0u || (wd & NW_FROZEN)) continue;
-                    const uint64_t p = (uint64_t)x | ((uint64_t)y << 21) | ((uint64_t)z << 42);
-                    if ((wd & NW_CLASS_MASK) == C_SOLID) {
-                        solid_xyz.push_back(p);
-                        solid_word.push_back(wd);
-                    } else {
-                        list_xyz.push_back(p);
-                        list_word.push_back(wd);
-                    }
-                }
-            }
-    }
-    if (list_xyz.size() + solid_xyz.size() >= (size_t)INT32_MAX / 27) {
-        free_all(h.get());
-        return fail(nullptr, MRLBM_ERR_INVALID_ARG, "too many boundary nodes");
-    }
-    h->n_list_pop = (int)list_xyz.size();
-    list_xyz.insert(list_xyz.end(), solid_xyz.begin(), solid_xyz.end());
-    list_word.insert(list_word.end(), solid_word.begin(), solid_word.end());
-    h->n_list = (int)list_xyz.size();
-    h->n_list_blocks = special_list_blocks(h->n_list);
-    const int nseg = (d.nz + h->lz - 1) / h->lz;
-    std::vector<int32_t> items;
-    for (int s = 0; s < nseg; ++s)
-        for (int t = 0; t < tiles; ++t)
-            if (!skip[t]) items.push_back(t | (s << 20));
-    h->n_items = (int)items.size();
-    h->n_ctas = std::max(1, std::min(h->n_items, resident));
 
     mrlbm_handle *H = h.get();
     const size_t mbytes = (size_t)h->fs * h->vbytes;
@@ -415,16 +576,7 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     CK(H, cudaMalloc(&h->m[1], mbytes));
     CK(H, cudaMemset(h->m[0], 0, mbytes));
     CK(H, cudaMemset(h->m[1], 0, mbytes));
-    if (any_special) {
-        CK(H, upload(&h->d_word, word.data(), word.size()));
-        CK(H, upload(&h->d_tile_slot, slot.data(), slot.size()));
-        if (n_special > 0) {
-            const size_t side_floats = (size_t)n_special * d.nz * TILE_X * h->tile_y * 16;
-            CK(H, cudaMalloc((void **)&h->d_side, side_floats * sizeof(float)));
-            CK(H, cudaMemset(h->d_side, 0, side_floats * sizeof(float)));
-        }
-    }
-    CK(H, upload(&h->d_items, items.data(), items.size()));
+    if (any_special) CK(H, upload(&h->d_word, word.data(), word.size()));
     for (int w = 0; w < g.n_walls; ++w) {
         const WallData &wd = g.wall[w];
         CK(H, upload(&h->d_wf[w][0], wd.nx.data(), wd.nx.size()));
@@ -445,13 +597,6 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     CK(H, cudaMemset(h->d_error, 0, sizeof(int)));
     CK(H, cudaMalloc((void **)&h->d_force_ring, (size_t)kRing * 10 * sizeof(double)));
     CK(H, cudaMalloc((void **)&h->d_diag_ring, (size_t)kRing * 2 * sizeof(double)));
-    CK(H, cudaMalloc((void **)&h->d_diag_part, (size_t)(h->n_ctas + h->n_list_blocks) * 2 * sizeof(double)));
-    if (h->n_list > 0) {
-        CK(H, upload(&h->d_list_xyz, list_xyz.data(), list_xyz.size()));
-        CK(H, upload(&h->d_list_word, list_word.data(), list_word.size()));
-        CK(H, upload(&h->d_row_base, row_base.data(), row_base.size()));
-        if (h->n_list_pop > 0) CK(H, cudaMalloc((void **)&h->d_popbuf, (size_t)h->n_list_pop * 27 * sizeof(float)));
-    }
     h->force_steps.assign(kRing, -1);
     h->diag_steps.assign(kRing, -1);
 
@@ -460,23 +605,9 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     a.m[1] = h->m[1];
     a.nxb = (d.nx + kXBlock - 1) / kXBlock;
     a.word = h->d_word;
-    a.items = h->d_items;
-    a.n_items = h->n_items;
-    a.tile_slot = h->d_tile_slot;
-    a.side = h->d_side;
-    a.list_xyz = h->d_list_xyz;
-    a.list_word = h->d_list_word;
-    a.n_list_pop = h->n_list_pop;
-    a.n_list = h->n_list;
-    a.popbuf = h->d_popbuf;
-    a.row_base = h->d_row_base;
     a.nx = d.nx;
     a.ny = d.ny;
     a.nz = d.nz;
-    a.tiles_x = h->tiles_x;
-    a.tiles_y = h->tiles_y;
-    a.tile_y = h->tile_y;
-    a.lz = h->lz;
     a.omega = h->der.omega;
     a.rho0 = d.rho0;
     a.u_max = d.u_max;
@@ -505,7 +636,13 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     a.tag_in = h->d_tag;
     a.tag_out = h->d_tag ? h->d_tag + 256 : nullptr;
     a.error = h->d_error;
-    CK(H, upload(&h->d_args, &a, 1));
+    CK(H, cudaMalloc((void **)&h->d_args, sizeof(StepArgs)));
+    {
+        int ty = 16, lz = 0;
+        default_tiling(ty, lz);
+        const int rc = setup_tiling(H, ty, lz);
+        if (rc != MRLBM_OK) return rc;
+    }
     CK(H, cudaDeviceSynchronize());
     *out = h.release();
     return MRLBM_OK;
@@ -513,6 +650,7 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
 
 int mrlbm_destroy(mrlbm_handle *h) {
     if (!h) return MRLBM_OK;
+    if (h->batch) return fail(h, MRLBM_ERR_STATE, "this handle belongs to a batch: use mrlbm_batch_destroy");
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (!h->host_only) free_all(h);
     delete h;
@@ -522,6 +660,7 @@ int mrlbm_destroy(mrlbm_handle *h) {
 int mrlbm_set_stream(mrlbm_handle *h, void *cuda_stream) {
     if (!h) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null handle");
     if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    if (h->batch) return fail(h, MRLBM_ERR_STATE, "this handle belongs to a batch: it runs on the batch stream");
     CK(h, cudaStreamSynchronize(h->stream));
     h->stream = cuda_stream ? (cudaStream_t)cuda_stream : h->own_stream;
     return MRLBM_OK;
@@ -592,40 +731,50 @@ int mrlbm_set_sampling(mrlbm_handle *h, int32_t force_every, int32_t diag_every)
 int mrlbm_step(mrlbm_handle *h, int32_t nsteps) {
     if (!h) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null handle");
     if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    if (h->batch) return fail(h, MRLBM_ERR_STATE, "this handle belongs to a batch: step it with mrlbm_batch_step");
     if (!h->initialized) return fail(h, MRLBM_ERR_STATE, "mrlbm_init / mrlbm_set_moments must come first");
     if (nsteps < 0) return fail(h, MRLBM_ERR_INVALID_ARG, "negative step count");
-    const int nb = (int)(h->geo.wall[0].list.size() + h->geo.wall[1].list.size());
-    const int nbf = (int)(h->geo.wall[0].fluid_list.size() + h->geo.wall[1].fluid_list.size());
-    for (int s = 0; s < nsteps; ++s) {
-        const int64_t it = h->step;
-        const bool fs = h->force_every > 0 && it % h->force_every == 0;
-        const bool ds = h->diag_every > 0 && it % h->diag_every == 0;
-        StepLaunch L;
-        L.ga = h->d_args;
-        L.parity = h->parity;
-        L.n_ctas = h->n_ctas;
-        if (fs) {
-            const int64_t slot = h->force_count % kRing;
-            L.force = h->d_force_ring + slot * 10;
-            CK(h, cudaMemsetAsync(L.force, 0, 10 * sizeof(double), h->stream));
-            h->force_steps[slot] = it;
-            ++h->force_count;
+    return step_handle(h, nsteps);
+}
+
+int mrlbm_autotune(mrlbm_handle *h, int32_t trial_steps, int32_t tile_out[3]) {
+    if (!h) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null handle");
+    if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    if (h->batch) return fail(h, MRLBM_ERR_STATE, "this handle belongs to a batch: use mrlbm_batch_autotune");
+    if (trial_steps < 1) return fail(h, MRLBM_ERR_INVALID_ARG, "need at least one trial step");
+    SavedState st;
+    int rc = save_state(h, st);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    CK(h, cudaEventCreate(&e0));
+    CK(h, cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_ty = h->tile_y, best_lz = h->lz;
+    for (int ty : {4, 8, 16}) {
+        for (int lz : lz_candidates(h->d.nz)) {
+            if ((rc = setup_tiling(h, ty, lz)) != MRLBM_OK) return rc;
+            if ((rc = step_handle(h, 1)) != MRLBM_OK) return rc;  // warm-up
+            CK(h, cudaEventRecord(e0, h->stream));
+            if ((rc = step_handle(h, trial_steps)) != MRLBM_OK) return rc;
+            CK(h, cudaEventRecord(e1, h->stream));
+            CK(h, cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CK(h, cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                best_ty = ty;
+                best_lz = h->lz;
+            }
         }
-        if (ds) L.diag_part = h->d_diag_part;
-        CK(h, launch_step(L, h->storage, h->tile_y, h->d_word != nullptr, h->stream));
-        if (h->n_list > 0)
-            CK(h, launch_special_list(L, h->storage, h->n_list_blocks, ds ? h->d_diag_part + 2 * h->n_ctas : nullptr,
-                                      h->stream));
-        if (nb > 0) CK(h, launch_wall(L, h->storage, nb + (fs ? nbf : 0), h->stream));
-        if (ds) {
-            const int64_t slot = h->diag_count % kRing;
-            CK(h, launch_diag_finalize(h->d_diag_part, h->n_ctas + (h->n_list > 0 ? h->n_list_blocks : 0),
-                                       h->d_diag_ring + slot * 2, h->stream));
-            h->diag_steps[slot] = it;
-            ++h->diag_count;
-        }
-        h->parity ^= 1;
-        ++h->step;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if ((rc = setup_tiling(h, best_ty, best_lz)) != MRLBM_OK) return rc;
+    if ((rc = restore_state(h, st)) != MRLBM_OK) return rc;
+    if (tile_out) {
+        tile_out[0] = TILE_X;
+        tile_out[1] = h->tile_y;
+        tile_out[2] = h->lz;
     }
     return MRLBM_OK;
 }
@@ -810,6 +959,342 @@ int mrlbm_step_periodic_noalloc(const float *m_in, float *m_out, int32_t nx, int
     std::string err;
     const int rc = noalloc_periodic_step(p, err);
     if (rc != MRLBM_OK) return fail(nullptr, rc, err);
+    return MRLBM_OK;
+}
+
+}  // extern "C"
+
+// ---- batches of independent cases (no counterpart in the reference) -------------------------
+
+namespace {
+
+int bfail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define BCK(call)                                                                  \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess) return bfail(MRLBM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+void batch_free_graphs(mrlbm_batch *b) {
+    for (auto &row : b->graph)
+        for (auto &g : row) {
+            if (g) cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
+void batch_free_tables(mrlbm_batch *b) {
+    batch_free_graphs(b);
+    for (void **p : {(void **)&b->d_cases, (void **)&b->d_items, (void **)&b->d_list_blocks,
+                     (void **)&b->d_wall_blocks, (void **)&b->d_ring, (void **)&b->d_slot, (void **)&b->d_ba}) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
+}
+
+// Tile every case with (ty, lz) and rebuild the merged work-item and block tables.
+int batch_set_tiling(mrlbm_batch *b, int ty, int lz) {
+    BCK(cudaStreamSynchronize(b->stream));
+    for (mrlbm_handle *h : b->h) {
+        const int rc = setup_tiling(h, ty, lz);
+        if (rc != MRLBM_OK) return rc;
+    }
+    batch_free_tables(b);
+    b->tile_y = ty;
+    b->lz = lz;
+    const int n = (int)b->h.size();
+    std::vector<const StepArgs *> cases(n);
+    std::vector<double *> ring(n);
+    std::vector<int2> items;
+    std::vector<int4> lblocks, wblocks;
+    for (int c = 0; c < n; ++c) {
+        mrlbm_handle *h = b->h[c];
+        cases[c] = h->d_args;
+        ring[c] = h->d_force_ring;
+        for (int32_t it : h->h_items) items.push_back(make_int2(c, it));
+        if (h->n_list > 0) {
+            const int first = (int)lblocks.size();
+            for (int k = 0; k < h->n_list_blocks; ++k) lblocks.push_back(make_int4(c, first, h->n_list_blocks, 0));
+        }
+        const int nw = (int)(h->geo.wall[0].list.size() + h->geo.wall[1].list.size() +
+                             h->geo.wall[0].fluid_list.size() + h->geo.wall[1].fluid_list.size());
+        if (nw > 0) {
+            const int first = (int)wblocks.size(), nblk = (nw + 127) / 128;
+            for (int k = 0; k < nblk; ++k) wblocks.push_back(make_int4(c, first, nblk, 0));
+        }
+    }
+    b->n_items = (int)items.size();
+    b->n_list_blocks = (int)lblocks.size();
+    b->n_wall_blocks = (int)wblocks.size();
+    int per_sm = step_kernel_max_ctas_per_sm(b->storage, ty);
+    if (per_sm <= 0) per_sm = 1;
+    b->n_ctas = std::max(1, std::min(b->n_items, per_sm * b->h[0]->n_sm));
+    auto up = [&](auto **dptr, const auto &v) -> cudaError_t {
+        using T = typename std::remove_reference<decltype(v)>::type::value_type;
+        if (v.empty()) return cudaSuccess;
+        cudaError_t e = cudaMalloc((void **)dptr, v.size() * sizeof(T));
+        if (e != cudaSuccess) return e;
+        return cudaMemcpy((void *)*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    };
+    BCK(up(&b->d_cases, cases));
+    BCK(up(&b->d_ring, ring));
+    BCK(up(&b->d_items, items));
+    BCK(up(&b->d_list_blocks, lblocks));
+    BCK(up(&b->d_wall_blocks, wblocks));
+    BCK(cudaMalloc((void **)&b->d_slot, sizeof(int)));
+    BCK(cudaMemset(b->d_slot, 0, sizeof(int)));
+    BatchArgs ba;
+    ba.cases = b->d_cases;
+    ba.items = b->d_items;
+    ba.n_items = b->n_items;
+    ba.list_blocks = b->d_list_blocks;
+    ba.wall_blocks = b->d_wall_blocks;
+    ba.force_ring = b->d_ring;
+    ba.force_slot = b->d_slot;
+    BCK(cudaMalloc((void **)&b->d_ba, sizeof(BatchArgs)));
+    BCK(cudaMemcpy(b->d_ba, &ba, sizeof(BatchArgs), cudaMemcpyHostToDevice));
+    BCK(prepare_step_batch(b->storage, ty));
+    return MRLBM_OK;
+}
+
+// The three batched launches of one step.
+int batch_launch(mrlbm_batch *b, int parity, int force) {
+    BCK(launch_step_batch(b->d_ba, parity, b->storage, b->tile_y, b->n_ctas, b->stream));
+    BCK(launch_special_list_batch(b->d_ba, parity, force, b->storage, b->n_list_blocks, b->stream));
+    BCK(launch_wall_batch(b->d_ba, parity, force, b->storage, b->n_wall_blocks, b->stream));
+    return MRLBM_OK;
+}
+
+int batch_graph(mrlbm_batch *b, int parity, int force, cudaGraphExec_t *out) {
+    if (!b->graph[parity][force]) {
+        cudaGraph_t g = nullptr;
+        BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = batch_launch(b, parity, force);
+        const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+        if (rc != MRLBM_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        BCK(ce);
+        const cudaError_t ie = cudaGraphInstantiate(&b->graph[parity][force], g, 0);
+        cudaGraphDestroy(g);
+        BCK(ie);
+    }
+    *out = b->graph[parity][force];
+    return MRLBM_OK;
+}
+
+// Advance every case one step with the batched kernels (graph replay or direct launches).
+int batch_step_once(mrlbm_batch *b, bool use_graph) {
+    const int64_t it = b->step;
+    const int force = b->force_every > 0 && it % b->force_every == 0;
+    if (force) {
+        const int64_t slot = b->force_count % kRing;
+        BCK(launch_batch_force_begin(b->d_ring, (int)b->h.size(), (int)slot, b->d_slot, b->stream));
+        for (mrlbm_handle *h : b->h) {
+            if (!h->geo.n_walls) continue;  // as mrlbm_set_sampling: no walls, no force samples
+            h->force_steps[slot] = it;
+            ++h->force_count;
+        }
+        ++b->force_count;
+    }
+    if (use_graph) {
+        cudaGraphExec_t g = nullptr;
+        const int rc = batch_graph(b, b->parity, force, &g);
+        if (rc != MRLBM_OK) return rc;
+        BCK(cudaGraphLaunch(g, b->stream));
+    } else {
+        const int rc = batch_launch(b, b->parity, force);
+        if (rc != MRLBM_OK) return rc;
+    }
+    b->parity ^= 1;
+    ++b->step;
+    for (mrlbm_handle *h : b->h) {
+        h->parity = b->parity;
+        h->step = b->step;
+    }
+    return MRLBM_OK;
+}
+
+int batch_check(mrlbm_batch *b) {
+    if (!b) return bfail(MRLBM_ERR_INVALID_ARG, "null batch");
+    for (mrlbm_handle *h : b->h)
+        if (!h->initialized) return bfail(MRLBM_ERR_STATE, "initialise every case of the batch first");
+    return MRLBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mrlbm_batch_create(const mrlbm_case_desc *descs, int32_t n, mrlbm_batch **out) {
+    if (!descs || !out || n <= 0) return bfail(MRLBM_ERR_INVALID_ARG, "need descriptors and n > 0");
+    *out = nullptr;
+    std::unique_ptr<mrlbm_batch> b(new mrlbm_batch());
+    auto cleanup = [&]() {
+        for (mrlbm_handle *h : b->h) {
+            h->batch = nullptr;
+            h->stream = h->own_stream;
+            mrlbm_destroy(h);
+        }
+        b->h.clear();
+        if (b->stream) cudaStreamDestroy(b->stream);
+    };
+    for (int i = 0; i < n; ++i) {
+        mrlbm_handle *h = nullptr;
+        const int rc = mrlbm_create(&descs[i], &h);
+        if (rc != MRLBM_OK) {
+            const std::string msg = "case " + std::to_string(i) + ": " + g_last_error;
+            cleanup();
+            return bfail(rc, msg);
+        }
+        b->h.push_back(h);
+        if (h->storage != b->h[0]->storage) {
+            cleanup();
+            return bfail(MRLBM_ERR_INVALID_ARG, "all cases of a batch must use the same moment storage");
+        }
+    }
+    b->storage = b->h[0]->storage;
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cleanup();
+        return bfail(MRLBM_ERR_CUDA, "cannot create the batch stream");
+    }
+    for (mrlbm_handle *h : b->h) {
+        cudaStreamSynchronize(h->stream);
+        h->stream = b->stream;
+        h->batch = b.get();
+    }
+    int ty = 16, lz = 0;
+    default_tiling(ty, lz);
+    const int rc = batch_set_tiling(b.get(), ty, lz);
+    if (rc != MRLBM_OK) {
+        const std::string msg = g_last_error;
+        batch_free_tables(b.get());
+        cleanup();
+        return bfail(rc, msg);
+    }
+    *out = b.release();
+    return MRLBM_OK;
+}
+
+int mrlbm_batch_destroy(mrlbm_batch *b) {
+    if (!b) return MRLBM_OK;
+    cudaStreamSynchronize(b->stream);
+    batch_free_tables(b);
+    for (mrlbm_handle *h : b->h) {
+        h->batch = nullptr;
+        h->stream = h->own_stream;
+        mrlbm_destroy(h);
+    }
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return MRLBM_OK;
+}
+
+int mrlbm_batch_size(const mrlbm_batch *b) { return b ? (int)b->h.size() : 0; }
+
+int mrlbm_batch_handle(mrlbm_batch *b, int32_t i, mrlbm_handle **out) {
+    if (!b || !out || i < 0 || i >= (int)b->h.size()) return bfail(MRLBM_ERR_INVALID_ARG, "bad batch index");
+    *out = b->h[i];
+    return MRLBM_OK;
+}
+
+int mrlbm_batch_set_sampling(mrlbm_batch *b, int32_t force_every) {
+    if (!b || force_every < 0) return bfail(MRLBM_ERR_INVALID_ARG, "bad batch sampling");
+    b->force_every = force_every;
+    for (mrlbm_handle *h : b->h) {
+        h->force_every = h->geo.n_walls ? force_every : 0;
+        h->diag_every = 0;
+    }
+    return MRLBM_OK;
+}
+
+int mrlbm_batch_step(mrlbm_batch *b, int32_t nsteps) {
+    int rc = batch_check(b);
+    if (rc != MRLBM_OK) return rc;
+    if (nsteps < 0) return bfail(MRLBM_ERR_INVALID_ARG, "negative step count");
+    for (int s = 0; s < nsteps; ++s)
+        if ((rc = batch_step_once(b, true)) != MRLBM_OK) return rc;
+    return MRLBM_OK;
+}
+
+int mrlbm_batch_step_sequential(mrlbm_batch *b, int32_t nsteps) {
+    int rc = batch_check(b);
+    if (rc != MRLBM_OK) return rc;
+    if (nsteps < 0) return bfail(MRLBM_ERR_INVALID_ARG, "negative step count");
+    for (int s = 0; s < nsteps; ++s) {
+        for (mrlbm_handle *h : b->h)
+            if ((rc = step_handle(h, 1)) != MRLBM_OK) return bfail(rc, g_last_error);
+        if (b->force_every > 0 && b->step % b->force_every == 0) ++b->force_count;
+        b->parity ^= 1;
+        ++b->step;
+    }
+    return MRLBM_OK;
+}
+
+int mrlbm_batch_sync(mrlbm_batch *b) {
+    if (!b) return bfail(MRLBM_ERR_INVALID_ARG, "null batch");
+    BCK(cudaStreamSynchronize(b->stream));
+    for (mrlbm_handle *h : b->h) {
+        const int rc = mrlbm_sync(h);
+        if (rc != MRLBM_OK) return rc;
+    }
+    return MRLBM_OK;
+}
+
+int mrlbm_batch_autotune(mrlbm_batch *b, int32_t trial_steps, int32_t tile_out[3]) {
+    int rc = batch_check(b);
+    if (rc != MRLBM_OK) return rc;
+    if (trial_steps < 1) return bfail(MRLBM_ERR_INVALID_ARG, "need at least one trial step");
+    BCK(cudaStreamSynchronize(b->stream));
+    std::vector<SavedState> saved(b->h.size());
+    for (size_t c = 0; c < b->h.size(); ++c)
+        if ((rc = save_state(b->h[c], saved[c])) != MRLBM_OK) return rc;
+    const int saved_parity = b->parity, saved_force = b->force_every;
+    const int64_t saved_step = b->step;
+    b->force_every = 0;
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    int max_nz = 0;
+    for (mrlbm_handle *h : b->h) max_nz = std::max(max_nz, h->d.nz);
+    float best = 1e30f;
+    int best_ty = b->tile_y, best_lz = b->lz;
+    for (int ty : {4, 8, 16}) {
+        for (int lz : lz_candidates(max_nz)) {
+            if ((rc = batch_set_tiling(b, ty, lz)) != MRLBM_OK) return rc;
+            if ((rc = batch_step_once(b, false)) != MRLBM_OK) return rc;  // warm-up
+            BCK(cudaEventRecord(e0, b->stream));
+            for (int s = 0; s < trial_steps; ++s)
+                if ((rc = batch_step_once(b, false)) != MRLBM_OK) return rc;
+            BCK(cudaEventRecord(e1, b->stream));
+            BCK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            BCK(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                best_ty = ty;
+                best_lz = lz;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if ((rc = batch_set_tiling(b, best_ty, best_lz)) != MRLBM_OK) return rc;
+    for (size_t c = 0; c < b->h.size(); ++c)
+        if ((rc = restore_state(b->h[c], saved[c])) != MRLBM_OK) return rc;
+    b->parity = saved_parity;
+    b->step = saved_step;
+    b->force_every = saved_force;
+    if (tile_out) {
+        tile_out[0] = TILE_X;
+        tile_out[1] = b->tile_y;
+        tile_out[2] = b->lz;
+    }
     return MRLBM_OK;
 }
 

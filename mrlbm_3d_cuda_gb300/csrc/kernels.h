@@ -64,6 +64,19 @@ struct StepArgs {
     const int32_t *row_base = nullptr;    // [slot][z][tile row]: first list entry of the row
 };
 
+// Several independent cases advanced together: one step-kernel launch over the work items of
+// every case, one node-list launch and one wall launch whose blocks each serve one case.
+// Lives in device memory; the kernels read each case's own StepArgs through `cases`.
+struct BatchArgs {
+    const StepArgs *const *cases = nullptr;  // device StepArgs of each case
+    const int2 *items = nullptr;             // {case, tile | z-segment << 20}
+    int n_items = 0;
+    const int4 *list_blocks = nullptr;       // per node-list block: {case, first block of the case, blocks, 0}
+    const int4 *wall_blocks = nullptr;       // per wall block: {case, first block of the case, blocks, 0}
+    double *const *force_ring = nullptr;     // per case: force ring of the case
+    const int *force_slot = nullptr;         // ring slot of the sampled step
+};
+
 // Per-step launch parameters.
 struct StepLaunch {
     const StepArgs *ga = nullptr;  // device copy of the handle's StepArgs
@@ -81,6 +94,13 @@ inline __host__ __device__ int64_t side_index(int slot, int x, int y, int z, int
 
 // storage: 0 f32, 1 f16, 2 bf16
 cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, bool special, cudaStream_t s);
+cudaError_t launch_step_batch(const BatchArgs *ba, int parity, int storage, int tile_y, int n_ctas, cudaStream_t s);
+cudaError_t prepare_step_batch(int storage, int tile_y);  // before capturing batched launches
+cudaError_t launch_special_list_batch(const BatchArgs *ba, int parity, int force, int storage, int n_blocks,
+                                      cudaStream_t s);
+cudaError_t launch_wall_batch(const BatchArgs *ba, int parity, int force, int storage, int n_blocks, cudaStream_t s);
+// Zero the slot of every case's force ring and publish the slot for the batched wall kernel.
+cudaError_t launch_batch_force_begin(double *const *ring, int n_cases, int slot, int *d_slot, cudaStream_t s);
 int step_kernel_smem_bytes(int tile_y);
 int step_kernel_max_ctas_per_sm(int storage, int tile_y);
 // Curved-wall closure + collision for the wall nodes of both walls, plus the force sums.

@@ -28,12 +28,15 @@ struct Mom {
 };
 
 // f_q = w_q rho [1 + 3 c.u + 4.5 (c_a c_b - delta_ab / 3) m_ab], second-order Hermite.
+// The scaled moments go through __fmul_rn, which is never fused into an FMA: the owner and
+// the rim copies of this function keep different subsets of the populations, and free
+// contraction of `scaled moment + sum` made the two round differently.
 __device__ __forceinline__ void reconstruct(const Mom &m, float f[27]) {
-    const float ux = 3.0f * m.ux, uy = 3.0f * m.uy, uz = 3.0f * m.uz;
-    const float xx = 4.5f * m.mxx, yy = 4.5f * m.myy, zz = 4.5f * m.mzz;
-    const float xy = 9.0f * m.mxy, xz = 9.0f * m.mxz, yz = 9.0f * m.myz;
+    const float ux = __fmul_rn(3.0f, m.ux), uy = __fmul_rn(3.0f, m.uy), uz = __fmul_rn(3.0f, m.uz);
+    const float xx = __fmul_rn(4.5f, m.mxx), yy = __fmul_rn(4.5f, m.myy), zz = __fmul_rn(4.5f, m.mzz);
+    const float xy = __fmul_rn(9.0f, m.mxy), xz = __fmul_rn(9.0f, m.mxz), yz = __fmul_rn(9.0f, m.myz);
     const float tr = xx + yy + zz;
-    const float p0 = 1.0f - kCs2 * tr;
+    const float p0 = __fmaf_rn(-kCs2, tr, 1.0f);
     const float r0 = m.rho * kW0, r1 = m.rho * kW1, r2 = m.rho * kW2, r3 = m.rho * kW3;
     f[0] = r0 * p0;
     const float ax = p0 + xx, ay = p0 + yy, az = p0 + zz;
@@ -121,15 +124,18 @@ __device__ __forceinline__ void evaluate(const float f[27], Mom &m) {
     m.myz = syz * inv;
 }
 
-// m_ab <- (1 - omega) m_ab + omega u_a u_b; rho and u are collision invariants.
+// m_ab <- (1 - omega) m_ab + omega u_a u_b; rho and u are collision invariants.  The rounding order is spelled out with
+// intrinsics: `a*b + c*d` has two possible FMA contractions, and leaving the choice to the
+// compiler let different kernel instantiations (tile heights) round differently.
 __device__ __forceinline__ void collide(Mom &m, float omega) {
     const float om1 = 1.0f - omega;
-    m.mxx = om1 * m.mxx + omega * m.ux * m.ux;
-    m.myy = om1 * m.myy + omega * m.uy * m.uy;
-    m.mzz = om1 * m.mzz + omega * m.uz * m.uz;
-    m.mxy = om1 * m.mxy + omega * m.ux * m.uy;
-    m.mxz = om1 * m.mxz + omega * m.ux * m.uz;
-    m.myz = om1 * m.myz + omega * m.uy * m.uz;
+    const float wx = __fmul_rn(omega, m.ux), wy = __fmul_rn(omega, m.uy), wz = __fmul_rn(omega, m.uz);
+    m.mxx = __fmaf_rn(wx, m.ux, __fmul_rn(om1, m.mxx));
+    m.myy = __fmaf_rn(wy, m.uy, __fmul_rn(om1, m.myy));
+    m.mzz = __fmaf_rn(wz, m.uz, __fmul_rn(om1, m.mzz));
+    m.mxy = __fmaf_rn(wx, m.uy, __fmul_rn(om1, m.mxy));
+    m.mxz = __fmaf_rn(wx, m.uz, __fmul_rn(om1, m.mxz));
+    m.myz = __fmaf_rn(wy, m.uz, __fmul_rn(om1, m.myz));
 }
 
 // ---------------------------------------------------------------------------------------

@@ -90,14 +90,23 @@ __device__ __forceinline__ int special_node(const StepArgs &a, int parity, bool 
 
 constexpr int kListThreads = 256;
 
-template <typename S>
-__global__ void __launch_bounds__(kListThreads) special_list_kernel(const StepArgs *__restrict__ ga, int parity,
-                                                                      int force, double *__restrict__ diag_part) {
+// BATCH: each block serves the case named by its entry in BatchArgs::list_blocks.
+template <typename S, bool BATCH>
+__global__ void __launch_bounds__(kListThreads)
+    special_list_kernel(const StepArgs *__restrict__ ga, const BatchArgs *__restrict__ ba, int parity, int force,
+                        double *__restrict__ diag_part) {
+    int b0 = blockIdx.x, nblk = gridDim.x;
+    if constexpr (BATCH) {
+        const int4 m = ba->list_blocks[blockIdx.x];
+        ga = ba->cases[m.x];
+        b0 = blockIdx.x - m.y;
+        nblk = m.z;
+    }
     const StepArgs &a = *ga;
     S *__restrict__ dst = (S *)a.m[parity ^ 1];
     const int n_pop = a.n_list_pop, n_all = a.n_list;
     double dm = 0.0, de = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_all; i += gridDim.x * blockDim.x) {
+    for (int i = b0 * blockDim.x + threadIdx.x; i < n_all; i += nblk * blockDim.x) {
         const uint64_t p = a.list_xyz[i];
         const int x = (int)(p & 0x1FFFFFu), y = (int)((p >> 21) & 0x1FFFFFu), z = (int)(p >> 42);
         const uint32_t w = a.list_word[i];
@@ -152,16 +161,36 @@ int special_list_blocks(int n_list) {
 }
 
 cudaError_t launch_special_list(const StepLaunch &l, int storage, int n_blocks, double *diag_part, cudaStream_t s) {
+    const int f = l.force != nullptr;
     switch (storage) {
         case MRLBM_STORAGE_F32:
-            special_list_kernel<float><<<n_blocks, kListThreads, 0, s>>>(l.ga, l.parity, l.force != nullptr, diag_part);
+            special_list_kernel<float, false><<<n_blocks, kListThreads, 0, s>>>(l.ga, nullptr, l.parity, f, diag_part);
             break;
         case MRLBM_STORAGE_F16:
-            special_list_kernel<__half><<<n_blocks, kListThreads, 0, s>>>(l.ga, l.parity, l.force != nullptr, diag_part);
+            special_list_kernel<__half, false><<<n_blocks, kListThreads, 0, s>>>(l.ga, nullptr, l.parity, f, diag_part);
             break;
         case MRLBM_STORAGE_BF16:
-            special_list_kernel<__nv_bfloat16>
-                <<<n_blocks, kListThreads, 0, s>>>(l.ga, l.parity, l.force != nullptr, diag_part);
+            special_list_kernel<__nv_bfloat16, false>
+                <<<n_blocks, kListThreads, 0, s>>>(l.ga, nullptr, l.parity, f, diag_part);
+            break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_special_list_batch(const BatchArgs *ba, int parity, int force, int storage, int n_blocks,
+                                      cudaStream_t s) {
+    if (n_blocks <= 0) return cudaSuccess;
+    switch (storage) {
+        case MRLBM_STORAGE_F32:
+            special_list_kernel<float, true><<<n_blocks, kListThreads, 0, s>>>(nullptr, ba, parity, force, nullptr);
+            break;
+        case MRLBM_STORAGE_F16:
+            special_list_kernel<__half, true><<<n_blocks, kListThreads, 0, s>>>(nullptr, ba, parity, force, nullptr);
+            break;
+        case MRLBM_STORAGE_BF16:
+            special_list_kernel<__nv_bfloat16, true>
+                <<<n_blocks, kListThreads, 0, s>>>(nullptr, ba, parity, force, nullptr);
             break;
         default: return cudaErrorInvalidValue;
     }

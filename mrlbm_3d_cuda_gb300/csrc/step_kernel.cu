@@ -136,9 +136,9 @@ __device__ __forceinline__ void gather_evaluate(const float *up, const float *fl
     m.ux = ((u.sx + c.sx) + d.sx) * inv;
     m.uy = ((u.sy + c.sy) + d.sy) * inv;
     m.uz = (u.s0 - d.s0) * inv;
-    m.mxx = ((u.sxx + c.sxx) + d.sxx) * inv - kCs2;
-    m.myy = ((u.syy + c.syy) + d.syy) * inv - kCs2;
-    m.mzz = (u.s0 + d.s0) * inv - kCs2;
+    m.mxx = __fmaf_rn((u.sxx + c.sxx) + d.sxx, inv, -kCs2);
+    m.myy = __fmaf_rn((u.syy + c.syy) + d.syy, inv, -kCs2);
+    m.mzz = __fmaf_rn(u.s0 + d.s0, inv, -kCs2);
     m.mxy = ((u.sxy + c.sxy) + d.sxy) * inv;
     m.mxz = (u.sx - d.sx) * inv;
     m.myz = (u.sy - d.sy) * inv;
@@ -213,30 +213,49 @@ __device__ __forceinline__ void nb_arrive(int id, int n) {
 // 1 + (k&1) / 3 + (k&1); a role can run at most one generation ahead on an id, so
 // consecutive generations never mix.  Counts are always the whole CTA (owner arrivals +
 // rim arrivals), so the rim work of the next plane overlaps the owners' emit.
-template <typename S, int TY, bool SPECIAL>
+template <typename S, int TY, bool SPECIAL, bool BATCH>
 __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
-    step_kernel(const StepArgs *__restrict__ ga, const int parity, double *__restrict__ force,
+    step_kernel(const StepArgs *__restrict__ ga, const BatchArgs *__restrict__ ba, const int parity,
                 double *__restrict__ diag_part) {
     using G = Geo<TY>;
     extern __shared__ float smem[];
     __shared__ double red[2][TY];
-    const S *__restrict__ src = (const S *)ga->m[parity];
-    S *__restrict__ dst = (S *)ga->m[parity ^ 1];
-    const int nxb = ga->nxb;
-    const int nx = ga->nx, ny = ga->ny, nz = ga->nz, lz = ga->lz, tiles_x = ga->tiles_x, n_items = ga->n_items;
-    const int32_t *__restrict__ items = ga->items;
-    const int32_t *__restrict__ tile_slot = ga->tile_slot;
-    const uint32_t *__restrict__ word = ga->word;
-    float *__restrict__ popbuf = ga->popbuf;
-    const int n_pop = ga->n_list_pop;
-    const int32_t *__restrict__ row_base = ga->row_base;
-    (void)force;  // boundary forces are integrated by the node-list and wall kernels
-    const float omega = ga->omega, rho0 = ga->rho0;
-    const StorageScale sc = ga->sc;
+    // per-case values: fixed for a single case, reloaded per work item in a batch
+    const S *__restrict__ src = nullptr;
+    S *__restrict__ dst = nullptr;
+    int nxb = 0, nx = 0, ny = 0, nz = 0, lz = 0, tiles_x = 0;
+    const int32_t *__restrict__ tile_slot = nullptr;
+    const uint32_t *__restrict__ word = nullptr;
+    float *__restrict__ popbuf = nullptr;
+    int n_pop = 0;
+    const int32_t *__restrict__ row_base = nullptr;
+    float omega = 1.f, rho0 = 1.f;
+    StorageScale sc;
+    int64_t plane = 0, zst = 0;  // lexicographic plane (node words), storage elements per z plane
+    auto load_case = [&](const StepArgs *__restrict__ c) {
+        src = (const S *)c->m[parity];
+        dst = (S *)c->m[parity ^ 1];
+        nxb = c->nxb;
+        nx = c->nx;
+        ny = c->ny;
+        nz = c->nz;
+        lz = c->lz;
+        tiles_x = c->tiles_x;
+        tile_slot = c->tile_slot;
+        word = c->word;
+        popbuf = c->popbuf;
+        n_pop = c->n_list_pop;
+        row_base = c->row_base;
+        omega = c->omega;
+        rho0 = c->rho0;
+        sc = c->sc;
+        plane = (int64_t)nx * ny;
+        zst = (int64_t)ny * nxb * 10 * kXBlock;
+    };
+    if constexpr (!BATCH) load_case(ga);
+    const int n_items = BATCH ? ba->n_items : ga->n_items;
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
     const bool owner = tid < G::NOWN;
-    const int64_t plane = (int64_t)nx * ny;                 // lexicographic plane (node words)
-    const int64_t zst = (int64_t)ny * nxb * 10 * kXBlock;  // storage elements per z plane
     const bool diag = diag_part != nullptr;
     float *const up_base = smem;
     float *const fl_base = smem + G::NUP * G::PLANE;
@@ -244,7 +263,14 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     double dmD = 0.0, deD = 0.0;
 
     for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
-        const int item = items[it];
+        int item;
+        if constexpr (BATCH) {
+            const int2 e = ba->items[it];
+            load_case(ba->cases[e.x]);
+            item = e.y;
+        } else {
+            item = ga->items[it];
+        }
         const int tile = item & 0xFFFFF, seg = item >> 20;
         const int tix = tile % tiles_x, tiy = tile / tiles_x;
         const int x0 = tix * TILE_X, y0 = tiy * TY;
@@ -446,25 +472,36 @@ __global__ void diag_finalize_kernel(const double *__restrict__ part, int n, dou
     }
 }
 
-template <typename S, int TY, bool SP>
-cudaError_t launch_t(const StepLaunch &l, cudaStream_t s) {
+// Opt the kernel into its dynamic shared memory once per process (never inside a stream capture:
+// batched launches are prepared before their graphs are captured).
+template <typename S, int TY, bool SP, bool BATCH>
+cudaError_t configure_t() {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(step_kernel<S, TY, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             Geo<TY>::SMEM);
+        cudaError_t e = cudaFuncSetAttribute(step_kernel<S, TY, SP, BATCH>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, Geo<TY>::SMEM);
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    step_kernel<S, TY, SP><<<l.n_ctas, Geo<TY>::NTH, Geo<TY>::SMEM, s>>>(l.ga, l.parity, l.force, l.diag_part);
+    return cudaSuccess;
+}
+
+template <typename S, int TY, bool SP, bool BATCH>
+cudaError_t launch_t(const StepArgs *ga, const BatchArgs *ba, int parity, double *diag_part, int n_ctas,
+                     cudaStream_t s) {
+    const cudaError_t e = configure_t<S, TY, SP, BATCH>();
+    if (e != cudaSuccess) return e;
+    step_kernel<S, TY, SP, BATCH><<<n_ctas, Geo<TY>::NTH, Geo<TY>::SMEM, s>>>(ga, ba, parity, diag_part);
     return cudaGetLastError();
 }
 
-template <typename S, bool SP>
-cudaError_t launch_s(const StepLaunch &l, int tile_y, cudaStream_t s) {
+template <typename S, bool SP, bool BATCH>
+cudaError_t launch_s(const StepArgs *ga, const BatchArgs *ba, int parity, double *diag_part, int n_ctas, int tile_y,
+                     cudaStream_t s) {
     switch (tile_y) {
-        case 4: return launch_t<S, 4, SP>(l, s);
-        case 8: return launch_t<S, 8, SP>(l, s);
-        case 16: return launch_t<S, 16, SP>(l, s);
+        case 4: return launch_t<S, 4, SP, BATCH>(ga, ba, parity, diag_part, n_ctas, s);
+        case 8: return launch_t<S, 8, SP, BATCH>(ga, ba, parity, diag_part, n_ctas, s);
+        case 16: return launch_t<S, 16, SP, BATCH>(ga, ba, parity, diag_part, n_ctas, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -472,8 +509,8 @@ cudaError_t launch_s(const StepLaunch &l, int tile_y, cudaStream_t s) {
 template <typename S, int TY>
 int occ_t() {
     int n = 0;
-    cudaFuncSetAttribute(step_kernel<S, TY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, Geo<TY>::SMEM);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<S, TY, true>, Geo<TY>::NTH, Geo<TY>::SMEM) !=
+    cudaFuncSetAttribute(step_kernel<S, TY, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, Geo<TY>::SMEM);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<S, TY, true, false>, Geo<TY>::NTH, Geo<TY>::SMEM) !=
         cudaSuccess)
         return 0;
     return n;
@@ -491,11 +528,47 @@ int occ_s(int ty) {
 }  // namespace
 
 cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, bool special, cudaStream_t s) {
+    const StepArgs *ga = l.ga;
     switch (storage) {
-        case MRLBM_STORAGE_F32: return special ? launch_s<float, true>(l, tile_y, s) : launch_s<float, false>(l, tile_y, s);
-        case MRLBM_STORAGE_F16: return special ? launch_s<__half, true>(l, tile_y, s) : launch_s<__half, false>(l, tile_y, s);
+        case MRLBM_STORAGE_F32:
+            return special ? launch_s<float, true, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s)
+                           : launch_s<float, false, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s);
+        case MRLBM_STORAGE_F16:
+            return special ? launch_s<__half, true, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s)
+                           : launch_s<__half, false, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s);
         case MRLBM_STORAGE_BF16:
-            return special ? launch_s<__nv_bfloat16, true>(l, tile_y, s) : launch_s<__nv_bfloat16, false>(l, tile_y, s);
+            return special
+                       ? launch_s<__nv_bfloat16, true, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s)
+                       : launch_s<__nv_bfloat16, false, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <typename S>
+cudaError_t prepare_s(int tile_y) {
+    switch (tile_y) {
+        case 4: return configure_t<S, 4, true, true>();
+        case 8: return configure_t<S, 8, true, true>();
+        case 16: return configure_t<S, 16, true, true>();
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t prepare_step_batch(int storage, int tile_y) {
+    switch (storage) {
+        case MRLBM_STORAGE_F32: return prepare_s<float>(tile_y);
+        case MRLBM_STORAGE_F16: return prepare_s<__half>(tile_y);
+        case MRLBM_STORAGE_BF16: return prepare_s<__nv_bfloat16>(tile_y);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_step_batch(const BatchArgs *ba, int parity, int storage, int tile_y, int n_ctas, cudaStream_t s) {
+    switch (storage) {
+        case MRLBM_STORAGE_F32: return launch_s<float, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
+        case MRLBM_STORAGE_F16: return launch_s<__half, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
+        case MRLBM_STORAGE_BF16:
+            return launch_s<__nv_bfloat16, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -666,7 +739,8 @@ int noalloc_periodic_step(const NoAllocStep &p, std::string &err) {
     double *part = (double *)(scratch + kNoAllocPartOffset);
     double *sums = (double *)(scratch + kNoAllocDiagOffset);
     if (p.diag_host) L.diag_part = part;
-    if ((e = launch_t<float, kNoAllocTileY, false>(L, p.stream)) != cudaSuccess)
+    if ((e = launch_t<float, kNoAllocTileY, false, false>(L.ga, nullptr, 0, L.diag_part, L.n_ctas, p.stream)) !=
+        cudaSuccess)
         return noalloc_cuda_fail(e, "step launch", err);
     if (p.diag_host) {
         if ((e = launch_diag_finalize(part, n_ctas, sums, p.stream)) != cudaSuccess)

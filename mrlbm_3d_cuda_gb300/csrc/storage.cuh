@@ -45,7 +45,7 @@ __device__ __forceinline__ Mom decode(const float v[10], float rho0, const Stora
         m.mxx = v[4]; m.myy = v[5]; m.mzz = v[6];
         m.mxy = v[7]; m.mxz = v[8]; m.myz = v[9];
     } else {
-        m.rho = rho0 + v[0] * sc.is[0];
+        m.rho = __fmaf_rn(v[0], sc.is[0], rho0);  // one rounding in every caller
         m.ux = v[1] * sc.is[1]; m.uy = v[2] * sc.is[1]; m.uz = v[3] * sc.is[1];
         m.mxx = v[4] * sc.is[2]; m.myy = v[5] * sc.is[2]; m.mzz = v[6] * sc.is[2];
         m.mxy = v[7] * sc.is[2]; m.mxz = v[8] * sc.is[2]; m.myz = v[9] * sc.is[2];

@@ -150,13 +150,23 @@ __device__ void closure_rotated(const StepArgs &a, float c, float s, uint32_t in
     }
 }
 
-template <typename S>
-__global__ void __launch_bounds__(128) wall_kernel(const StepArgs *__restrict__ ga, int parity, double *force) {
+// BATCH: each block serves the case named by its entry in BatchArgs::wall_blocks; the force
+// sums of a sampled step go to that case's ring slot BatchArgs::force_slot.
+template <typename S, bool BATCH>
+__global__ void __launch_bounds__(128)
+    wall_kernel(const StepArgs *__restrict__ ga, const BatchArgs *__restrict__ ba, int parity, double *force) {
+    int b0 = blockIdx.x;
+    if constexpr (BATCH) {
+        const int4 m = ba->wall_blocks[blockIdx.x];
+        ga = ba->cases[m.x];
+        b0 = blockIdx.x - m.y;
+        force = force ? ba->force_ring[m.x] + (int64_t)(*ba->force_slot) * 10 : nullptr;
+    }
     const StepArgs &a = *ga;
     const int nb0 = a.wall[0].nb, nb1 = a.wall[1].nb;
     const int nbf0 = force ? a.wall[0].nbf : 0, nbf1 = force ? a.wall[1].nbf : 0;
     const int n_total = nb0 + nb1 + nbf0 + nbf1;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = b0 * blockDim.x + threadIdx.x;
     const int64_t plane = (int64_t)a.nx * a.ny;
     double acc[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
     if (i < nb0 + nb1) {
@@ -247,11 +257,40 @@ cudaError_t launch_wall(const StepLaunch &l, int storage, int n_total, cudaStrea
     if (n_total <= 0) return cudaSuccess;
     const int blocks = (n_total + 127) / 128;
     switch (storage) {
-        case MRLBM_STORAGE_F32: wall_kernel<float><<<blocks, 128, 0, s>>>(l.ga, l.parity, l.force); break;
-        case MRLBM_STORAGE_F16: wall_kernel<__half><<<blocks, 128, 0, s>>>(l.ga, l.parity, l.force); break;
-        case MRLBM_STORAGE_BF16: wall_kernel<__nv_bfloat16><<<blocks, 128, 0, s>>>(l.ga, l.parity, l.force); break;
+        case MRLBM_STORAGE_F32: wall_kernel<float, false><<<blocks, 128, 0, s>>>(l.ga, nullptr, l.parity, l.force); break;
+        case MRLBM_STORAGE_F16: wall_kernel<__half, false><<<blocks, 128, 0, s>>>(l.ga, nullptr, l.parity, l.force); break;
+        case MRLBM_STORAGE_BF16:
+            wall_kernel<__nv_bfloat16, false><<<blocks, 128, 0, s>>>(l.ga, nullptr, l.parity, l.force);
+            break;
         default: return cudaErrorInvalidValue;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wall_batch(const BatchArgs *ba, int parity, int force, int storage, int n_blocks, cudaStream_t s) {
+    if (n_blocks <= 0) return cudaSuccess;
+    // any non-null pointer switches force accumulation on; the kernel takes the case's slot
+    double *f = force ? reinterpret_cast<double *>(1) : nullptr;
+    switch (storage) {
+        case MRLBM_STORAGE_F32: wall_kernel<float, true><<<n_blocks, 128, 0, s>>>(nullptr, ba, parity, f); break;
+        case MRLBM_STORAGE_F16: wall_kernel<__half, true><<<n_blocks, 128, 0, s>>>(nullptr, ba, parity, f); break;
+        case MRLBM_STORAGE_BF16:
+            wall_kernel<__nv_bfloat16, true><<<n_blocks, 128, 0, s>>>(nullptr, ba, parity, f);
+            break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+namespace {
+__global__ void batch_force_begin_kernel(double *const *ring, int n_cases, int slot, int *d_slot) {
+    for (int i = threadIdx.x; i < n_cases * 10; i += blockDim.x) ring[i / 10][(int64_t)slot * 10 + i % 10] = 0.0;
+    if (threadIdx.x == 0) *d_slot = slot;
+}
+}  // namespace
+
+cudaError_t launch_batch_force_begin(double *const *ring, int n_cases, int slot, int *d_slot, cudaStream_t s) {
+    batch_force_begin_kernel<<<1, 256, 0, s>>>(ring, n_cases, slot, d_slot);
     return cudaGetLastError();
 }
 

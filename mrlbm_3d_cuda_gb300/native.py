@@ -97,6 +97,16 @@ _SIGS = {
     "mrlbm_checkpoint_save": (C.c_int, [C.c_void_p, C.c_char_p]),
     "mrlbm_checkpoint_load": (C.c_int, [C.c_void_p, C.c_char_p]),
     "mrlbm_write_vti": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "mrlbm_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "mrlbm_batch_create": (C.c_int, [C.POINTER(CaseDesc), C.c_int32, C.POINTER(C.c_void_p)]),
+    "mrlbm_batch_destroy": (C.c_int, [C.c_void_p]),
+    "mrlbm_batch_size": (C.c_int, [C.c_void_p]),
+    "mrlbm_batch_handle": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "mrlbm_batch_set_sampling": (C.c_int, [C.c_void_p, C.c_int32]),
+    "mrlbm_batch_step": (C.c_int, [C.c_void_p, C.c_int32]),
+    "mrlbm_batch_step_sequential": (C.c_int, [C.c_void_p, C.c_int32]),
+    "mrlbm_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "mrlbm_batch_sync": (C.c_int, [C.c_void_p]),
     "mrlbm_step_periodic_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float,
                                               C.c_float, C.c_void_p, C.c_void_p]),
 }

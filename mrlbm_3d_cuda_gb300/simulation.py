@@ -36,15 +36,20 @@ class Case:
 class Simulation:
     """One MR-LBM case resident on the current CUDA device."""
 
-    def __init__(self, case: Case | N.CaseDesc, init: bool = True, host_only: bool = False):
+    def __init__(self, case: Case | N.CaseDesc, init: bool = True, host_only: bool = False,
+                 _handle: C.c_void_p | None = None):
         if isinstance(case, N.CaseDesc):
             case = Case(case)
         self.case = case
         L = N.lib()
-        h = C.c_void_p()
         desc = N.CaseDesc.from_buffer_copy(case.desc)
-        create = L.mrlbm_create_host if host_only else L.mrlbm_create
-        N.check(create(C.byref(desc), C.byref(h)))
+        self._owned = _handle is None
+        if _handle is None:
+            h = C.c_void_p()
+            create = L.mrlbm_create_host if host_only else L.mrlbm_create
+            N.check(create(C.byref(desc), C.byref(h)))
+        else:
+            h = _handle
         if host_only:
             init = False
         self._h = h
@@ -58,7 +63,8 @@ class Simulation:
     # ---- lifecycle ----------------------------------------------------------------------
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
-            N.lib().mrlbm_destroy(self._h)
+            if getattr(self, "_owned", True):
+                N.lib().mrlbm_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -75,6 +81,13 @@ class Simulation:
 
     def _ck(self, rc):
         return N.check(rc, self._h)
+
+    def autotune(self, trial_steps: int = 5) -> tuple:
+        """Pick the fastest tile height / z-segment (results are tiling independent)."""
+        t = (C.c_int32 * 3)()
+        self._ck(N.lib().mrlbm_autotune(self._h, int(trial_steps), t))
+        self.info = self.get_info()
+        return tuple(t)
 
     def get_info(self) -> N.Info:
         info = N.Info()
@@ -181,3 +194,57 @@ class Simulation:
 
     def write_vti(self, path: str):
         self._ck(N.lib().mrlbm_write_vti(self._h, str(path).encode()))
+
+
+class Batch:
+    """Independent cases advanced together by batched, graph-replayed launches
+    (mrlbm_batch_*).  `cases[i]` is a :class:`Simulation` view of case i for init, moments and
+    forces; step the cases only through the batch."""
+
+    def __init__(self, descs: Sequence[N.CaseDesc]):
+        L = N.lib()
+        arr = (N.CaseDesc * len(descs))(*[N.CaseDesc.from_buffer_copy(d) for d in descs])
+        b = C.c_void_p()
+        N.check(L.mrlbm_batch_create(arr, len(descs), C.byref(b)))
+        self._b = b
+        self.cases = []
+        for i, d in enumerate(descs):
+            h = C.c_void_p()
+            N.check(L.mrlbm_batch_handle(b, i, C.byref(h)))
+            self.cases.append(Simulation(d, init=False, _handle=h))
+        self.n_nodes = sum(c.n for c in self.cases)
+
+    def __len__(self):
+        return len(self.cases)
+
+    def close(self):
+        if getattr(self, "_b", None) is not None and self._b.value:
+            for c in self.cases:
+                c.close()
+            N.lib().mrlbm_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_sampling(self, force_every: int):
+        N.check(N.lib().mrlbm_batch_set_sampling(self._b, int(force_every)))
+
+    def step(self, n: int = 1):
+        N.check(N.lib().mrlbm_batch_step(self._b, int(n)))
+
+    def step_sequential(self, n: int = 1):
+        N.check(N.lib().mrlbm_batch_step_sequential(self._b, int(n)))
+
+    def autotune(self, trial_steps: int = 3) -> tuple:
+        t = (C.c_int32 * 3)()
+        N.check(N.lib().mrlbm_batch_autotune(self._b, int(trial_steps), t))
+        for c in self.cases:
+            c.info = c.get_info()
+        return tuple(t)
+
+    def sync(self):
+        N.check(N.lib().mrlbm_batch_sync(self._b))
