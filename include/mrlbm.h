@@ -190,9 +190,29 @@ int mrlbm_get_force_history(mrlbm_handle *h, int32_t max_steps, int64_t *steps, 
 int mrlbm_get_diagnostics(mrlbm_handle *h, int32_t max_steps, int64_t *steps, double *values, int32_t *n_out);
 
 /* ---- files in the reference formats --------------------------------------------------------- */
-int mrlbm_checkpoint_save(mrlbm_handle *h, const char *path); /* restart.bin layout */
+/* restart.bin (restart/restart_io.cu:3-92): int32 step count, the 10 moment arrays (rho - rho0
+ * first) in the tiled IDX_BLOCK order, then the six face-population arrays of its 8 x 8 x 4
+ * blocks (rebuilt here from the moments, which is what they hold after a reference step).
+ * Loading takes the moments and the step count; the face arrays carry no other state. */
+int mrlbm_checkpoint_save(mrlbm_handle *h, const char *path);
 int mrlbm_checkpoint_load(mrlbm_handle *h, const char *path);
-int mrlbm_write_vti(mrlbm_handle *h, const char *path);       /* data<10000000+it>.vti layout */
+/* data<10000000+it>.vti (output/saveData.cu:42-231): rho, ux, uy, uz with NaN velocity on
+ * solid nodes; annulus cases write rho, uz, u_theta, u_radial (velocities / u_max). */
+int mrlbm_write_vti(mrlbm_handle *h, const char *path);
+/* master.pvd listing data<10000000+it>.vti for it = 0, macr_save, ... <= max_iter
+ * (output/saveData.cu:3-40). */
+int mrlbm_write_master_pvd(const char *path, int32_t macr_save, int32_t max_iter);
+/* forces.dat `iter Fx Fy Fz` and mass_flux.dat `iter m` of wall `wall`, %.16f
+ * (statistics/stat_header.cuh:16-51); either path may be NULL.  append = 0 rewrites the
+ * files from every sample still in the device ring, append = 1 adds the samples taken since
+ * the previous call. */
+int mrlbm_write_forces(mrlbm_handle *h, int32_t wall, const char *forces_path, const char *mass_path, int32_t append);
+/* Time-averaged wall pressure over the steps start..end (inclusive; start < 0 switches it off),
+ * sampled after each step like compute_surface_pressure (cases/cylinder/cylinder_kernels.cu:
+ * 238-283); set before stepping, it restarts the average. */
+int mrlbm_set_pressure_window(mrlbm_handle *h, int64_t start, int64_t end);
+/* pressure.dat `theta z Cp` rows per wall node (cases/cylinder/cylinder_kernels.cuh:251-285). */
+int mrlbm_write_pressure(mrlbm_handle *h, int32_t wall, const char *path);
 
 /* ---- allocation-free step (no counterpart in the reference) ------------------------------------
  * One time step of a fully periodic box (no walls, no inlet / outlet) from m_in to m_out,

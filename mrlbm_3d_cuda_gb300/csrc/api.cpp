@@ -15,88 +15,15 @@
 
 #include <cuda_runtime.h>
 
-#include "kernels.h"
-#include "lattice_tables.h"
-#include "mrlbm_internal.h"
+#include "handle.h"
 
 using namespace mrlbm;
 
-namespace {
+namespace mrlbm {
 thread_local std::string g_last_error;
-constexpr int kRing = 65536;  // sampled steps kept on the device (forces, diagnostics)
-}  // namespace
+}  // namespace mrlbm
 
-struct mrlbm_handle {
-    mrlbm_case_desc d{};
-    Derived der{};
-    Geometry geo;
-    std::string err;
-    bool host_only = false;
-    int dev = 0, n_sm = 0;
-    cudaStream_t own_stream = nullptr, stream = nullptr;
-    int storage = 0, vbytes = 4;
-    StorageScale sc{};
-    int64_t n = 0, fs = 0;
-    void *m[2] = {nullptr, nullptr};
-    int parity = 0;
-    bool initialized = false;
-    int64_t step = 0;
-    // step-kernel configuration
-    int tile_y = 8, lz = 32, tiles_x = 0, tiles_y = 0, n_items = 0, n_ctas = 0;
-    int64_t n_fluid = 0;
-    uint32_t *d_word = nullptr;
-    int32_t *d_items = nullptr, *d_tile_slot = nullptr;
-    float *d_side = nullptr;
-    int n_special = 0;
-    // non-bulk node list handled by the node-list kernel
-    uint64_t *d_list_xyz = nullptr;
-    uint32_t *d_list_word = nullptr;
-    int32_t *d_row_base = nullptr;
-    float *d_popbuf = nullptr;
-    int n_list_pop = 0, n_list = 0, n_list_blocks = 0;
-    // walls
-    float *d_wf[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
-    uint32_t *d_wm[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-    int64_t *d_wl[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-    uint32_t *d_tag = nullptr;  // [512]: in masks then out masks
-    StepArgs args{};
-    StepArgs *d_args = nullptr;
-    std::vector<int32_t> h_items;   // host copy of the work items
-    mrlbm_batch *batch = nullptr;   // owning batch, if any
-    int *d_error = nullptr;
-    // sampling
-    int force_every = 0, diag_every = 0;
-    double *d_force_ring = nullptr, *d_diag_ring = nullptr, *d_diag_part = nullptr;
-    std::vector<int64_t> force_steps, diag_steps;
-    int64_t force_count = 0, diag_count = 0;
-    // staging
-    float *d_stage = nullptr;
-    size_t stage_bytes = 0;
-};
-
-// Independent cases advanced together: every step is one persistent step-kernel launch over
-// the work items of all cases, one node-list launch and one wall launch, replayed from CUDA
-// graphs (one per ping-pong parity and force sampling).
-struct mrlbm_batch {
-    std::vector<mrlbm_handle *> h;
-    cudaStream_t stream = nullptr;
-    int storage = 0, tile_y = 16, lz = 0;
-    int parity = 0;
-    int64_t step = 0;
-    int force_every = 0;
-    int64_t force_count = 0;  // sampled steps so far (the ring slot of the cases with walls)
-    // device tables (BatchArgs and what it points to)
-    const StepArgs **d_cases = nullptr;
-    int2 *d_items = nullptr;
-    int4 *d_list_blocks = nullptr, *d_wall_blocks = nullptr;
-    double **d_ring = nullptr;
-    int *d_slot = nullptr;
-    BatchArgs *d_ba = nullptr;
-    int n_items = 0, n_ctas = 0, n_list_blocks = 0, n_wall_blocks = 0;
-    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [parity][force]
-};
-
-namespace {
+namespace mrlbm {
 
 int fail(mrlbm_handle *h, int code, const std::string &msg) {
     if (h) h->err = msg;
@@ -111,11 +38,6 @@ int cuda_fail(mrlbm_handle *h, cudaError_t e, const char *what) {
     return fail(h, code, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define CK(h, call)                                         \
-    do {                                                    \
-        cudaError_t e_ = (call);                            \
-        if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
-    } while (0)
 
 template <typename T>
 cudaError_t upload(T **dptr, const T *host, size_t count) {
@@ -154,6 +76,8 @@ void free_all(mrlbm_handle *h) {
     f(h->d_diag_ring);
     f(h->d_diag_part);
     f(h->d_stage);
+    f(h->d_ps_avg[0]);
+    f(h->d_ps_avg[1]);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
 }
 
@@ -344,6 +268,15 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
             CK(h, launch_special_list(L, h->storage, h->n_list_blocks, ds ? h->d_diag_part + 2 * h->n_ctas : nullptr,
                                       h->stream));
         if (nb > 0) CK(h, launch_wall(L, h->storage, nb + (fs ? nbf : 0), h->stream));
+        if (h->ps_start >= 0 && it >= h->ps_start && it <= h->ps_end) {
+            // statistics window: the post-step state (buffer parity ^ 1), as the reference's
+            // post_process_step samples it
+            ++h->ps_count;
+            for (int w = 0; w < h->geo.n_walls; ++w)
+                CK(h, launch_surface_pressure(h->d_args, h->parity ^ 1, h->storage, w,
+                                              (int)h->geo.wall[w].list.size(), h->d_ps_avg[w], h->ps_count,
+                                              h->stream));
+        }
         if (ds) {
             const int64_t slot = h->diag_count % kRing;
             CK(h, launch_diag_finalize(h->d_diag_part, h->n_ctas + (h->n_list > 0 ? h->n_list_blocks : 0),
@@ -929,19 +862,6 @@ int mrlbm_get_diagnostics(mrlbm_handle *h, int32_t max_steps, int64_t *steps, do
     }
     *n_out = (int32_t)n;
     return MRLBM_OK;
-}
-
-int mrlbm_checkpoint_save(mrlbm_handle *h, const char *path) {
-    (void)path;
-    return fail(h, MRLBM_ERR_UNSUPPORTED, "checkpoint writer not built yet");
-}
-int mrlbm_checkpoint_load(mrlbm_handle *h, const char *path) {
-    (void)path;
-    return fail(h, MRLBM_ERR_UNSUPPORTED, "checkpoint reader not built yet");
-}
-int mrlbm_write_vti(mrlbm_handle *h, const char *path) {
-    (void)path;
-    return fail(h, MRLBM_ERR_UNSUPPORTED, "vti writer not built yet");
 }
 
 int mrlbm_step_periodic_noalloc(const float *m_in, float *m_out, int32_t nx, int32_t ny, int32_t nz, float omega,

@@ -1,0 +1,115 @@
+// Host-side state behind the C ABI: the handle (one case on the device) and the batch.
+// Shared by the host translation units of the library (api.cpp, output.cpp).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "lattice_tables.h"
+#include "mrlbm_internal.h"
+
+namespace mrlbm {
+extern thread_local std::string g_last_error;
+constexpr int kRing = 65536;  // sampled steps kept on the device (forces, diagnostics)
+}  // namespace mrlbm
+
+using mrlbm::BatchArgs;
+using mrlbm::Derived;
+using mrlbm::Geometry;
+using mrlbm::StepArgs;
+using mrlbm::StorageScale;
+
+struct mrlbm_handle {
+    mrlbm_case_desc d{};
+    Derived der{};
+    Geometry geo;
+    std::string err;
+    bool host_only = false;
+    int dev = 0, n_sm = 0;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    int storage = 0, vbytes = 4;
+    StorageScale sc{};
+    int64_t n = 0, fs = 0;
+    void *m[2] = {nullptr, nullptr};
+    int parity = 0;
+    bool initialized = false;
+    int64_t step = 0;
+    // step-kernel configuration
+    int tile_y = 8, lz = 32, tiles_x = 0, tiles_y = 0, n_items = 0, n_ctas = 0;
+    int64_t n_fluid = 0;
+    uint32_t *d_word = nullptr;
+    int32_t *d_items = nullptr, *d_tile_slot = nullptr;
+    float *d_side = nullptr;
+    int n_special = 0;
+    // non-bulk node list handled by the node-list kernel
+    uint64_t *d_list_xyz = nullptr;
+    uint32_t *d_list_word = nullptr;
+    int32_t *d_row_base = nullptr;
+    float *d_popbuf = nullptr;
+    int n_list_pop = 0, n_list = 0, n_list_blocks = 0;
+    // walls
+    float *d_wf[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    uint32_t *d_wm[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    int64_t *d_wl[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    uint32_t *d_tag = nullptr;  // [512]: in masks then out masks
+    StepArgs args{};
+    StepArgs *d_args = nullptr;
+    std::vector<int32_t> h_items;   // host copy of the work items
+    mrlbm_batch *batch = nullptr;   // owning batch, if any
+    int *d_error = nullptr;
+    // sampling
+    int force_every = 0, diag_every = 0;
+    double *d_force_ring = nullptr, *d_diag_ring = nullptr, *d_diag_part = nullptr;
+    std::vector<int64_t> force_steps, diag_steps;
+    int64_t forces_written = 0;  // force samples already written by mrlbm_write_forces
+    // time-averaged wall pressure (pressure.dat)
+    int64_t ps_start = -1, ps_end = -1;
+    int ps_count = 0;
+    double *d_ps_avg[2] = {nullptr, nullptr};
+    int64_t force_count = 0, diag_count = 0;
+    // staging
+    float *d_stage = nullptr;
+    size_t stage_bytes = 0;
+};
+
+// Independent cases advanced together: every step is one persistent step-kernel launch over
+// the work items of all cases, one node-list launch and one wall launch, replayed from CUDA
+// graphs (one per ping-pong parity and force sampling).
+struct mrlbm_batch {
+    std::vector<mrlbm_handle *> h;
+    cudaStream_t stream = nullptr;
+    int storage = 0, tile_y = 16, lz = 0;
+    int parity = 0;
+    int64_t step = 0;
+    int force_every = 0;
+    int64_t force_count = 0;  // sampled steps so far (the ring slot of the cases with walls)
+    // device tables (BatchArgs and what it points to)
+    const StepArgs **d_cases = nullptr;
+    int2 *d_items = nullptr;
+    int4 *d_list_blocks = nullptr, *d_wall_blocks = nullptr;
+    double **d_ring = nullptr;
+    int *d_slot = nullptr;
+    BatchArgs *d_ba = nullptr;
+    int n_items = 0, n_ctas = 0, n_list_blocks = 0, n_wall_blocks = 0;
+    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [parity][force]
+};
+
+
+
+namespace mrlbm {
+// Record an error on the handle (if any) and as this thread's last error; returns `code`.
+int fail(mrlbm_handle *h, int code, const std::string &msg);
+int cuda_fail(mrlbm_handle *h, cudaError_t e, const char *what);
+// Device staging buffer of at least `bytes` (FP32 host-layout conversions).
+int ensure_stage(mrlbm_handle *h, size_t bytes);
+}  // namespace mrlbm
+
+#define CK(h, call)                                                    \
+    do {                                                               \
+        cudaError_t e_ = (call);                                       \
+        if (e_ != cudaSuccess) return mrlbm::cuda_fail(h, e_, #call);  \
+    } while (0)

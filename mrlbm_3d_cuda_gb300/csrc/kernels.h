@@ -127,6 +127,17 @@ cudaError_t launch_convert(const void *src, void *dst_a, void *dst_b, float *f32
                            int layout, int nx, int ny, int nz, int storage, const StorageScale &sc, int dir,
                            cudaStream_t s);
 
+// Reference-format outputs (output_kernels.cu).
+// Floats of one halo face array of the reference layout (axis 0: X_WEST / X_EAST, 1: Y, 2: Z).
+int64_t halo_face_floats(int nx, int ny, int nz, int axis);
+// The six face-population arrays of a restart.bin (X_WEST, X_EAST, Y_SOUTH, Y_NORTH, Z_BACK,
+// Z_FRONT) rebuilt from the moments in buffer `parity`.
+cudaError_t launch_halo_export(const StepArgs *ga, int parity, int storage, int64_t n, float *const faces[6],
+                               cudaStream_t s);
+// Accumulate the wall pressure of the state in buffer `buf` into a running mean over n_avg samples.
+cudaError_t launch_surface_pressure(const StepArgs *ga, int buf, int storage, int wall, int nb, double *avg, int n_avg,
+                                    cudaStream_t s);
+
 // Allocation-free periodic step (mrlbm_step_periodic_noalloc).  Everything the step kernel
 // needs besides the caller's two moment buffers lives in one fixed array in the library's
 // device image, laid out as:

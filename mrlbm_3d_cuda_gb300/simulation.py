@@ -195,6 +195,54 @@ class Simulation:
     def write_vti(self, path: str):
         self._ck(N.lib().mrlbm_write_vti(self._h, str(path).encode()))
 
+    def write_forces(self, forces_path: str | None, mass_path: str | None = None, wall: int = 0,
+                     append: bool = False):
+        """forces.dat (`iter Fx Fy Fz`) and mass_flux.dat (`iter m`) of the sampled steps."""
+        enc = (lambda p: str(p).encode() if p is not None else None)
+        self._ck(N.lib().mrlbm_write_forces(self._h, int(wall), enc(forces_path), enc(mass_path), int(bool(append))))
+
+    def set_pressure_window(self, start: int, end: int):
+        """Average the wall pressure over steps start..end (start < 0: off)."""
+        self._ck(N.lib().mrlbm_set_pressure_window(self._h, int(start), int(end)))
+
+    def write_pressure(self, path: str, wall: int = 0):
+        self._ck(N.lib().mrlbm_write_pressure(self._h, int(wall), str(path).encode()))
+
+    def run_reference_outputs(self, out_dir: str, max_iter: int, macr_save: int, stat_start: int, stat_end: int,
+                              checkpoint_save: int = 0):
+        """The reference's time loop with its output cadence (main.cu:21-35, simulation.cu:121-159):
+        iterations 0..max_iter; data<10000000+it>.vti every macr_save iterations (master.pvd
+        lists them); checkpoint/restart.bin (+ restart_step.txt) every checkpoint_save
+        iterations after the first; forces / mass flux sampled and the wall pressure averaged
+        over stat_start..stat_end, written as forces.dat, mass_flux.dat and pressure.dat."""
+        import os
+        os.makedirs(out_dir, exist_ok=True)
+        write_master_pvd(os.path.join(out_dir, "master.pvd"), macr_save, max_iter)
+        walls = self.desc.geometry != N.GEOM_NONE
+        start = int(self.get_info().step)
+        if walls:
+            self.set_pressure_window(stat_start, stat_end)
+        for it in range(start, max_iter + 1):
+            stats = walls and stat_start <= it <= stat_end
+            self.set_sampling(1 if stats else 0, 0)
+            self.step(1)
+            if checkpoint_save and it > start and it % checkpoint_save == 0:
+                os.makedirs(os.path.join(out_dir, "checkpoint"), exist_ok=True)
+                self.checkpoint_save(os.path.join(out_dir, "checkpoint", "restart.bin"))
+                with open(os.path.join(out_dir, "checkpoint", "restart_step.txt"), "w") as f:
+                    f.write(f"{it + 1}\n")
+            if macr_save and it % macr_save == 0:
+                self.write_vti(os.path.join(out_dir, f"data{10000000 + it}.vti"))
+        self.set_sampling(0, 0)
+        if walls:
+            self.write_forces(os.path.join(out_dir, "forces.dat"), os.path.join(out_dir, "mass_flux.dat"))
+            self.write_pressure(os.path.join(out_dir, "pressure.dat"))
+
+
+def write_master_pvd(path: str, macr_save: int, max_iter: int):
+    """master.pvd listing data<10000000+it>.vti for it = 0, macr_save, ... <= max_iter."""
+    N.check(N.lib().mrlbm_write_master_pvd(str(path).encode(), int(macr_save), int(max_iter)))
+
 
 class Batch:
     """Independent cases advanced together by batched, graph-replayed launches

@@ -11,7 +11,10 @@ per step) are reduced here to a fixture small enough to commit:
   * every node that is not plain bulk fluid (walls, BCFLUID, inlet / outlet faces) plus a
     seeded random sample of 40,000 nodes, all 10 moments, by tiled index;
   * per-field max |m|, sum m and sum m^2 over the whole grid (FP64);
-  * the forces.dat rows.
+  * the forces.dat rows;
+  * 5,000 seeded positions of each of the six face-population arrays that follow the moments
+    in restart.bin (X_WEST, X_EAST, Y_SOUTH, Y_NORTH, Z_BACK, Z_FRONT, core/index.cuh:42-79),
+    with their values.
 
 Run on the GPU machine from the repository root:
     python oracle/ref_gpu.py stage cyl_n10 --steps 10          (where the reference tree is)
@@ -36,7 +39,8 @@ def read_restart(path: Path, n: int):
     raw = path.read_bytes()
     it = int(np.frombuffer(raw[:4], dtype=np.int32)[0])
     m = np.frombuffer(raw[4:4 + 40 * n], dtype=np.float32).reshape(10, n)
-    return it, m
+    halo = np.frombuffer(raw[4 + 40 * n:], dtype=np.float32)
+    return it, m, halo
 
 
 def main(tag: str, out: str):
@@ -50,7 +54,17 @@ def main(tag: str, out: str):
     n = desc.nx * desc.ny * desc.nz
     restart = next((d / "run").rglob("restart.bin"))
     forces = np.loadtxt(next((d / "run").rglob("forces.dat")), ndmin=2)
-    it, m = read_restart(restart, n)
+    it, m, halo = read_restart(restart, n)
+    nbk = (desc.nx // 8) * (desc.ny // 8) * (desc.nz // 4)
+    face_len = [32 * nbk * 9] * 4 + [64 * nbk * 9] * 2
+    assert halo.size == sum(face_len), (halo.size, face_len)
+    hrng = np.random.default_rng(7)
+    halo_pos, halo_val, off = [], [], 0
+    for ln in face_len:
+        pos = np.sort(hrng.choice(ln, 5000, replace=False))
+        halo_pos.append(pos)
+        halo_val.append(halo[off + pos])
+        off += ln
     assert it == cfg["steps"] + 1, (it, cfg)
     sim = Simulation(desc, host_only=True)
     types = sim.node_types(layout=N.LAYOUT_REF_TILED)
@@ -62,7 +76,8 @@ def main(tag: str, out: str):
     np.savez_compressed(
         out, steps=np.int64(it), idx=idx.astype(np.int32), moments=m[:, idx],
         field_max=np.abs(m64).max(axis=1), field_sum=m64.sum(axis=1), field_sumsq=(m64 * m64).sum(axis=1),
-        forces=forces, nxyz=np.array([desc.nx, desc.ny, desc.nz], dtype=np.int32))
+        forces=forces, nxyz=np.array([desc.nx, desc.ny, desc.nz], dtype=np.int32),
+        halo_pos=np.stack(halo_pos).astype(np.int64), halo_val=np.stack(halo_val))
     print(f"{out}: {it} steps, {idx.size} sampled nodes, {forces.shape[0]} force rows")
 
 
