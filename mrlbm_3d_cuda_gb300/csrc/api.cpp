@@ -414,8 +414,6 @@ int mrlbm_case_desc_finalize(mrlbm_case_desc *d) {
         return fail(nullptr, MRLBM_ERR_INVALID_ARG, "grid too large");
     if (d->storage < 0 || d->storage > 2) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "bad storage");
     if (d->geometry < 0 || d->geometry > 2) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "bad geometry");
-    if (d->neumann_current_update)
-        return fail(nullptr, MRLBM_ERR_UNSUPPORTED, "NEUMANN_CURRENT_UPDATE outlet is not built");
     if (!(d->rho0 > 0.f)) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "rho0 must be positive");
     if (d->omega <= 0.f && !(d->re > 0.f)) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "need re > 0 or omega > 0");
     if (d->geometry == MRLBM_GEOM_NONE && d->omega <= 0.f && !(d->length > 0.f))

@@ -23,6 +23,42 @@
 namespace mrlbm {
 namespace {
 
+// Density and velocity from a full set of 27 populations.
+__device__ __forceinline__ Mom rho_u_of(const float *f) {
+    float r = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+    for (int q = 0; q < 27; ++q) {
+        r += f[q];
+        jx += f[q] * (float)cxq(q);
+        jy += f[q] * (float)cyq(q);
+        jz += f[q] * (float)czq(q);
+    }
+    Mom m;
+    const float inv = 1.0f / r;
+    m.rho = r;
+    m.ux = jx * inv;
+    m.uy = jy * inv;
+    m.uz = jz * inv;
+    m.mxx = m.myy = m.mzz = m.mxy = m.mxz = m.myz = 0.f;
+    return m;
+}
+
+// Post-stream density and velocity of node (x, y, z): its 27 populations pulled from the
+// stored moments of the neighbours, on the grid that wraps in every axis.
+template <typename S>
+__device__ __noinline__ Mom pulled_rho_u(const StepArgs &a, const S *__restrict__ src, int x, int y, int z) {
+    float f[27];
+#pragma unroll 1
+    for (int q = 0; q < 27; ++q) {
+        const int xs = (x - cxq(q) + a.nx) % a.nx, ys = (y - cyq(q) + a.ny) % a.ny, zs = (z - czq(q) + a.nz) % a.nz;
+        const Mom mq = load_mom<S>(src, aos_index(xs, ys, zs, a.nxb, a.ny), a.rho0, a.sc);
+        float g[27];
+        reconstruct(mq, g);
+        f[q] = g[q];
+    }
+    return rho_u_of(f);
+}
+
 // Closure of one listed node from its pulled populations `fl`.  Returns 0 when the node is
 // not stored here (wall nodes: the wall kernel finishes them), 1 to store the collided moments
 // `m`, 2 to store them and count the node in the fluid diagnostics.
@@ -57,8 +93,17 @@ __device__ __forceinline__ int special_node(const StepArgs &a, int parity, bool 
             c.rho0 = a.rho0;
             c.convective = a.convective;
             c.self_prev = prev;
-            if (class_walls(cls) & 2u) c.west_prev = load_mom<S>(src, aos_index(x - 1, y, z, a.nxb, a.ny), a.rho0, a.sc);
-            else c.west_prev = prev;
+            c.west_prev = prev;
+            if (class_walls(cls) & 2u) {
+                if (a.current_update) {
+                    // NEUMANN_CURRENT_UPDATE (boundaries.cuh:96-161): post-stream rho, u of the
+                    // x-1 neighbour and of the node itself instead of their stored moments
+                    c.west_prev = pulled_rho_u<S>(a, src, x - 1, y, z);
+                    c.self_prev = rho_u_of(fl);
+                } else {
+                    c.west_prev = load_mom<S>(src, aos_index(x - 1, y, z, a.nxb, a.ny), a.rho0, a.sc);
+                }
+            }
             Mom o = prev;
             if (planar_closure(cls, fl, c, o)) m = o;
         }

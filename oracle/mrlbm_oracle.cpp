@@ -386,10 +386,40 @@ struct Oracle {
     // ---------------- closures ------------------------------------------------------------
     // update_neumaan_density_velocity (boundaries.cuh:163-199): pre-stream x-1 neighbour,
     // blended with the node itself by |u_x| when the outlet is convective.
-    void neumann(int64_t i, T &rho, T &ux, T &uy, T &uz) const {
-        const M10<T> a = load(i - 1);
+    // With NEUMANN_CURRENT_UPDATE (current_update_neumaan_density_velocity, boundaries.cuh:96-161)
+    // both are the post-stream sums instead: of the x-1 neighbour's streamed populations and
+    // of the node's own `p`, accumulated in q order.
+    M10<T> streamed_rho_u(const T *f) const {
+        M10<T> m{};
+        T r = 0, jx = 0, jy = 0, jz = 0;
+        for (int q = 0; q < 27; ++q) {
+            r += f[q];
+            jx += f[q] * (T)CX[q];
+            jy += f[q] * (T)CY[q];
+            jz += f[q] * (T)CZ[q];
+        }
+        const T inv = (T)1 / r;
+        m.rho = r;
+        m.ux = jx * inv;
+        m.uy = jy * inv;
+        m.uz = jz * inv;
+        return m;
+    }
+
+    void neumann(int64_t i, const T *p, T &rho, T &ux, T &uy, T &uz) const {
+        M10<T> a = load(i - 1);
+        M10<T> b = load(i);
+        if (d.neumann_current_update) {
+            const int x = (int)((i - 1) % nx), y = (int)(((i - 1) / nx) % ny), z = (int)((i - 1) / ((int64_t)nx * ny));
+            T f[27];
+            for (int q = 0; q < 27; ++q) {
+                const int xs = (x - CX[q] + nx) % nx, ys = (y - CY[q] + ny) % ny, zs = (z - CZ[q] + nz) % nz;
+                f[q] = pops[27 * idx(xs, ys, zs) + q];
+            }
+            a = streamed_rho_u(f);
+            b = streamed_rho_u(p);
+        }
         if (d.convective_outlet) {
-            const M10<T> b = load(i);
             const T uc = std::sqrt(a.ux * a.ux);
             rho = (T)((1.0 - (double)uc) * (double)b.rho + (double)(uc * a.rho));
             ux = (T)((1.0 - (double)uc) * (double)b.ux + (double)(uc * a.ux));
@@ -430,7 +460,7 @@ struct Oracle {
                 const T mxyI = ((p[7] + p[19] + p[21]) - (p[13] + p[23] + p[26])) * iv;
                 const T mxzI = ((p[9] + p[19] + p[23]) - (p[15] + p[21] + p[26])) * iv;
                 const T myzI = (p[11] + p[12] - p[17] - p[18] + p[19] - p[21] - p[23] + p[26]) * iv;
-                neumann(i, rho, ux, uy, uz);
+                neumann(i, p, rho, ux, uy, uz);
                 mxx = ux * ux;
                 myy = ((T)6 * myyI * rI - (T)6 * mzzI * rI + (T)5 * uy * uy * rho + (T)5 * uz * uz * rho) / ((T)10 * rho);
                 mzz = (-(T)6 * myyI * rI + (T)6 * mzzI * rI + (T)5 * uy * uy * rho + (T)5 * uz * uz * rho) / ((T)10 * rho);
@@ -520,7 +550,7 @@ struct Oracle {
             for (int k = 1; k < 4; ++k) side = e.ss[k] > 0 ? side + p[e.sq[k]] : side - p[e.sq[k]];
             const T sideI = e.side ? side * iv : (T)0;
             if (e.east) {
-                neumann(i, rho, ux, uy, uz);
+                neumann(i, p, rho, ux, uy, uz);
             } else {
                 rho = e.sign > 0 ? (T)36 * rI * (one + mI - mI * O) / ((T)24 + O)
                                  : (T)36 * rI * (one - mI + mI * O) / ((T)24 + O);
@@ -542,7 +572,7 @@ struct Oracle {
         for (const auto &k : K) {
             if (k.c != c) continue;
             if (k.east) {
-                neumann(i, rho, ux, uy, uz);
+                neumann(i, p, rho, ux, uy, uz);
             } else {
                 T rI = 0;
                 for (int j = 0; j < 8; ++j) rI += p[k.rq[j]];

@@ -125,6 +125,20 @@ def test_channel_with_cylinder_walls_and_edges(cuda_device):
     assert_forces(res, 0, comps=(0, 1, 3, 4))
 
 
+@pytest.mark.parametrize("convective", [False, True])
+def test_outlet_current_update(cuda_device, convective):
+    """NEUMANN_CURRENT_UPDATE: the outlet takes the post-stream rho, u of its x-1 neighbour
+    (and of itself when convective) instead of their stored moments."""
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    desc = cases.cylinder_channel(64, 40, 12, 10, 24.3, 19.7, 0.05, 60.0, convective=convective)
+    desc.neumann_current_update = 1
+    res = run_pair(desc, 6, N.INIT_REST, fp64=False)
+    assert_fields(res, 0.05, strict=True)
+    res = run_pair(desc, 40, N.INIT_REST)
+    assert_fields(res, 0.05)
+
+
 @pytest.mark.parametrize("steps", [8, 160])
 def test_reference_cylinder_case(cuda_device, steps):
     """The reference's shipped case (convective outlet, periodic y) from its own initial
