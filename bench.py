@@ -113,8 +113,28 @@ def dist_info():
     return rank, world, local
 
 
+def reduce_max(values):
+    """Element-wise max over all ranks (identity without a process group): every rank's
+    timings are replaced by the slowest rank's."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def replica_value(n_nodes: int, steps: int, seconds: float, world: int) -> float:
+    """Whole-job MLUPS of `world` replicas, each advancing n_nodes for `steps` steps, timed by
+    the slowest one."""
+    return world * n_nodes * steps / seconds / 1e6
+
+
 def cpu_baseline(n: int, slab: int, steps: int, bits: int = 32):
-    """Oracle (CPU restatement of the reference step) on an n x n x slab piece of the TGV."""
+    """Oracle (CPU restatement of the reference step, FP32 or FP64) on an n x n x slab piece of
+    the TGV, all host threads."""
     import oracle
     from mrlbm_3d_cuda_gb300 import cases
     from mrlbm_3d_cuda_gb300 import native as N
@@ -215,12 +235,9 @@ def run_batch(args):
     with ClockSampler(local) as clk:
         t_batch = timed(b.step)
     t_seq = timed(b.step_sequential)
-    if world > 1:
-        tt = torch.tensor([t_batch, t_seq], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_batch, t_seq = float(tt[0]), float(tt[1])
-    value = world * n_nodes * args.steps / t_batch / 1e6
-    seq_value = world * n_nodes * args.steps / t_seq / 1e6
+    t_batch, t_seq = reduce_max([t_batch, t_seq])
+    value = replica_value(n_nodes, args.steps, t_batch, world)
+    seq_value = replica_value(n_nodes, args.steps, t_seq, world)
 
     # end to end: upload every case's field from pinned memory, step with force sampling,
     # read back every case's force history and final field
@@ -238,7 +255,7 @@ def run_batch(args):
         c.moments(out=hb.numpy())
     b.sync()
     barrier()
-    e2e_s = time.perf_counter() - t
+    e2e_s = reduce_max([time.perf_counter() - t])[0]
     in_bytes = sum(hb.numel() * 4 for hb in hosts)
     peak, peak_kind = measured_peaks()
     line = {
@@ -256,7 +273,7 @@ def run_batch(args):
                      "peak": peak, "unit": "GB/s",
                      "frac": n_nodes * B_ALG[storage] * args.steps / t_batch / 1e9 / peak, "peak_kind": peak_kind,
                      "bytes_per_lup": B_ALG[storage], "traffic": None},
-        "e2e": {"value": world * n_nodes * args.steps / e2e_s / 1e6, "unit": "MLUPS",
+        "e2e": {"value": replica_value(n_nodes, args.steps, e2e_s, world), "unit": "MLUPS",
                 "h2d_bytes_per_step": in_bytes / args.steps, "d2h_bytes_per_step": (in_bytes + 80 * len(descs) * args.steps) / args.steps},
         "gpu_launches": 3 * args.steps,
         "clocks": clk.summary(),
@@ -315,13 +332,9 @@ def run_ours(args):
         sim.step(args.steps)
         ev1.record(stream)
         barrier()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max([ev0.elapsed_time(ev1)])[0]
     ms_step = ms / args.steps
-    value = world * n_nodes * args.steps / (ms * 1e-3) / 1e6
+    value = replica_value(n_nodes, args.steps, ms * 1e-3, world)
     kernel_ms = ms_step  # one step-kernel launch per step, back to back on one stream
 
     # ---- end-to-end through the C ABI with host buffers -----------------------------------
@@ -337,12 +350,8 @@ def run_ours(args):
     _, diag = sim.diagnostics(e2e_steps)
     sim.moments(out=hv)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * n_nodes * e2e_steps / e2e_s / 1e6
+    e2e_s = reduce_max([time.perf_counter() - t0])[0]
+    e2e_value = replica_value(n_nodes, e2e_steps, e2e_s, world)
     sim.set_sampling(0, 0)
     assert np.isfinite(diag).all()
 
@@ -369,7 +378,7 @@ def run_ours(args):
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(min(args.n, 128), 8, args.cpu_steps)
+        line["cpu_baseline"] = cpu_baseline(min(args.n, 128), 8, args.cpu_steps, bits=64)
     sim.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -384,7 +393,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f32", choices=list(STORAGE))
-    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--size", dest="n", type=int, default=256, help="TGV grid edge (n^3)")
     ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder", "batch"])
     ap.add_argument("--batch-cases", type=int, default=64)
     ap.add_argument("--no-autotune", action="store_true")

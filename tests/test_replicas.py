@@ -1,0 +1,67 @@
+"""Multi-GPU path: replicas only (one independent case per rank, no data exchange).  The
+rank logic of bench.py — max over ranks of the timings, whole-job MLUPS, rank 0 alone
+printing — is exercised here with world-size-2 gloo process groups on the CPU."""
+from __future__ import annotations
+
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank: int, world: int, port: int, out):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    sys.path.insert(0, ROOT)
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        got = bench.reduce_max([1.0 + rank, 10.0 - rank, 0.5])
+        out.put((rank, got, bench.replica_value(1000, 10, got[0], world)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_reduce_max_and_whole_job_value_with_gloo():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, got, value in res:
+        assert got == [2.0, 10.0, 0.5], (rank, got)  # slowest rank's timing, on every rank
+        assert value == pytest.approx(2 * 1000 * 10 / 2.0 / 1e6)
+
+
+def test_reference_arm_prints_once_under_torchrun(built):
+    """`bench.py --impl reference` launched like the multi-GPU bench: rank 0 alone measures
+    and prints one JSON line; the other rank exits 0 without work."""
+    port = free_port()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
+           "--gpus", "2", "--steps", "2", "--warmup", "1", "--size", "32", "--ref-slab", "4"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600,
+                       env={**os.environ, "OMP_NUM_THREADS": "2"})
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["unit"] == "MLUPS"
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
