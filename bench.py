@@ -285,6 +285,85 @@ def run_batch(args):
         torch.distributed.destroy_process_group()
 
 
+def shedding_stats(fx, fy, d, u, nz, rho0=1.0):
+    """Cd (mean), rms Cl and Strouhal number from per-step wall forces (second half of the run)."""
+    if len(fx) < 4:
+        return float("nan"), float("nan"), float("nan")
+    half = len(fx) // 2
+    q = 0.5 * rho0 * u * u * d * nz
+    cd = float(np.mean(fx[half:]) / q)
+    cl = fy[half:] / q
+    cl_rms = float(np.sqrt(np.mean((cl - cl.mean()) ** 2)))
+    spec = np.abs(np.fft.rfft(cl - cl.mean()))
+    freq = np.fft.rfftfreq(len(cl), d=1.0)
+    k = int(np.argmax(spec[1:]) + 1) if len(spec) > 1 else 0
+    st = float(freq[k] * d / u) if k else float("nan")
+    return cd, cl_rms, st
+
+
+def run_c5(args):
+    """C5: 1024 x 512 x 256 cylinder, D = 64, Re = 3900, u = 0.05 (1 + 1 % noise): FP16 moment
+    storage (FP32 collision, FP64 force sums) against an FP32-storage run of the same case;
+    MLUPS of the FP16 run, Cd / rms Cl / St of both."""
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    stats, value, ms_step, clocks = {}, None, None, None
+    for st in ("f16", "f32"):
+        desc = cases.c5_turbulent_cylinder(STORAGE[st], re=args.re)
+        sim = Simulation(desc, init=False)
+        sim.set_stream(stream.cuda_stream)
+        if args.c5_init == "noisy":
+            sim.init(N.INIT_NOISY_UNIFORM, (0.05, 0.0, 0.0, 0.01, 1234))
+        else:
+            sim.init(N.INIT_REST)
+        sim.set_sampling(1, 1000)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        done, diverged, ms = 0, None, 0.0
+        with ClockSampler(local) as clk:
+            while done < args.steps:  # chunks of 1000 steps, each checked for a non-finite state
+                k = min(1000, args.steps - done)
+                ev0.record(stream)
+                sim.step(k)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                ms += ev0.elapsed_time(ev1)
+                done += k
+                if not np.isfinite(sim.diagnostics()[1]).all():
+                    diverged = done
+                    break
+        _, f = sim.force_history(done)
+        good = np.isfinite(f[:, 0, :2]).all(axis=1)
+        n_ok = int(np.argmin(good)) if not good.all() else len(good)
+        stats[st] = shedding_stats(f[:n_ok, 0, 0], f[:n_ok, 0, 1], desc.d_wall[0], desc.u_max, desc.nz)
+        stats[st] += (diverged,)
+        ms_done = done
+        if st == "f16":
+            n_nodes = desc.nx * desc.ny * desc.nz
+            value, ms_step, clocks = replica_value(n_nodes, ms_done, ms * 1e-3, 1), ms / ms_done, clk.summary()
+            workload = (f"cylinder {desc.nx}x{desc.ny}x{desc.nz}, D={desc.d_wall[0]:.0f}, Re={args.re:g}, u=0.05, "
+                        f"start: {'uniform +1% noise' if args.c5_init == 'noisy' else 'rest'}, tau={1 / desc.omega:.5f}")
+        sim.close()
+    (cd16, cl16, st16, div16), (cd32, cl32, st32, div32) = stats["f16"], stats["f32"]
+    line = {
+        "metric": "MLUPS (D3Q27 MR-LBM, 1024x512x256 cylinder, FP16 storage)", "value": value,
+        "unit": "MLUPS", "n_gpus": 1, "steps": args.steps, "warmup": 0, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16", "data": "synthetic",
+        "config": {"workload": workload, "storage": "f16 vs f32",
+                   "f16": {"cd": cd16, "cl_rms": cl16, "st": st16, "diverged_at_step": div16},
+                   "f32": {"cd": cd32, "cl_rms": cl32, "st": st32, "diverged_at_step": div32},
+                   "cd_rel_err": cd16 / cd32 - 1, "cl_rms_rel_err": cl16 / cl32 - 1, "st_rel_err": st16 / st32 - 1,
+                   "statistics": "second half of the run; St from the Cl spectrum peak"},
+        "gpu_launches": 3 * args.steps, "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_info()
@@ -394,8 +473,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f32", choices=list(STORAGE))
     ap.add_argument("--size", dest="n", type=int, default=256, help="TGV grid edge (n^3)")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder", "batch"])
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder", "batch", "c5"])
     ap.add_argument("--batch-cases", type=int, default=64)
+    ap.add_argument("--re", type=float, default=3900.0, help="Reynolds number of the c5 workload")
+    ap.add_argument("--c5-init", default="noisy", choices=["noisy", "rest"])
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--diameter", type=int, default=16)
     ap.add_argument("--ref-slab", type=int, default=8)
@@ -406,6 +487,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "c5":
+        run_c5(args)
     else:
         run_ours(args)
 

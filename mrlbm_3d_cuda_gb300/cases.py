@@ -135,9 +135,9 @@ def c4_batch(n: int = 64, seed: int = 1234, storage: int = N.STORAGE_F32) -> lis
     return out
 
 
-def c5_turbulent_cylinder(storage: int = N.STORAGE_F16) -> N.CaseDesc:
+def c5_turbulent_cylinder(storage: int = N.STORAGE_F16, re: float = 3900.0) -> N.CaseDesc:
     """Large cylinder: 1024 x 512 x 256, D = 64 at (256, 256), Re = 3900, U = 0.05."""
-    return cylinder_channel(1024, 512, 256, 64, 256.0, 256.0, 0.05, 3900.0, storage=storage)
+    return cylinder_channel(1024, 512, 256, 64, 256.0, 256.0, 0.05, re, storage=storage)
 
 
 def tgv_params(desc: N.CaseDesc):
