@@ -58,6 +58,7 @@ void free_all(mrlbm_handle *h) {
     f(h->m[1]);
     f(h->d_word);
     f(h->d_items);
+    f(h->d_args_sp);
     f(h->d_tile_slot);
     f(h->d_side);
     f(h->d_list_xyz);
@@ -79,6 +80,9 @@ void free_all(mrlbm_handle *h) {
     f(h->d_ps_avg[0]);
     f(h->d_ps_avg[1]);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    if (h->side_stream) cudaStreamDestroy(h->side_stream);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
 }
 
 int64_t node_index_for_layout(const mrlbm_handle *h, int64_t lex, int layout) {
@@ -199,13 +203,19 @@ int setup_tiling(mrlbm_handle *h, int ty, int lz) {
     h->n_list = (int)list_xyz.size();
     h->n_list_blocks = special_list_blocks(h->n_list);
     const int nseg = (d.nz + h->lz - 1) / h->lz;
-    std::vector<int32_t> items;
+    // tiles without boundary nodes go to the bulk variant of the step kernel, the others to
+    // the variant that reads node words: two launches, each over its own items
+    std::vector<int32_t> items, items_sp;
     for (int s = 0; s < nseg; ++s)
         for (int t = 0; t < tiles; ++t)
-            if (!skip[t]) items.push_back(t | (s << 20));
+            if (!skip[t]) (slot[t] >= 0 ? items_sp : items).push_back(t | (s << 20));
     h->n_items = (int)items.size();
-    h->n_ctas = std::max(1, std::min(h->n_items, resident));
+    h->n_items_sp = (int)items_sp.size();
+    h->n_ctas = h->n_items ? std::max(1, std::min(h->n_items, resident)) : 0;
+    h->n_ctas_sp = h->n_items_sp ? std::max(1, std::min(h->n_items_sp, resident)) : 0;
     h->h_items = items;
+    h->h_items_sp = items_sp;
+    items.insert(items.end(), items_sp.begin(), items_sp.end());
 
     if (h->d_word) {
         CK(h, upload(&h->d_tile_slot, slot.data(), slot.size()));
@@ -216,7 +226,8 @@ int setup_tiling(mrlbm_handle *h, int ty, int lz) {
         }
     }
     CK(h, upload(&h->d_items, items.data(), items.size()));
-    CK(h, cudaMalloc((void **)&h->d_diag_part, (size_t)(h->n_ctas + h->n_list_blocks) * 2 * sizeof(double)));
+    CK(h, cudaMalloc((void **)&h->d_diag_part,
+                     (size_t)(h->n_ctas + h->n_ctas_sp + h->n_list_blocks) * 2 * sizeof(double)));
     if (h->n_list > 0) {
         CK(h, upload(&h->d_list_xyz, list_xyz.data(), list_xyz.size()));
         CK(h, upload(&h->d_list_word, list_word.data(), list_word.size()));
@@ -239,6 +250,11 @@ int setup_tiling(mrlbm_handle *h, int ty, int lz) {
     a.tile_y = h->tile_y;
     a.lz = h->lz;
     CK(h, cudaMemcpy(h->d_args, &a, sizeof(StepArgs), cudaMemcpyHostToDevice));
+    StepArgs asp = a;
+    asp.items = h->d_items ? h->d_items + h->n_items : nullptr;
+    asp.n_items = h->n_items_sp;
+    if (!h->d_args_sp) CK(h, cudaMalloc((void **)&h->d_args_sp, sizeof(StepArgs)));
+    CK(h, cudaMemcpy(h->d_args_sp, &asp, sizeof(StepArgs), cudaMemcpyHostToDevice));
     return MRLBM_OK;
 }
 
@@ -263,9 +279,23 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
             ++h->force_count;
         }
         if (ds) L.diag_part = h->d_diag_part;
-        CK(h, launch_step(L, h->storage, h->tile_y, h->d_word != nullptr, h->stream));
+        if (h->n_items_sp > 0) {
+            // boundary tiles on the side stream, concurrently with the bulk tiles: their CTAs
+            // fill the SMs the bulk launch leaves idle in its last wave
+            StepLaunch Ls = L;
+            Ls.ga = h->d_args_sp;
+            Ls.n_ctas = h->n_ctas_sp;
+            Ls.diag_part = ds ? h->d_diag_part + 2 * h->n_ctas : nullptr;
+            CK(h, cudaEventRecord(h->ev_fork, h->stream));
+            CK(h, cudaStreamWaitEvent(h->side_stream, h->ev_fork, 0));
+            CK(h, launch_step(Ls, h->storage, h->tile_y, true, h->side_stream));
+            CK(h, cudaEventRecord(h->ev_join, h->side_stream));
+        }
+        if (h->n_items > 0) CK(h, launch_step(L, h->storage, h->tile_y, false, h->stream));
+        if (h->n_items_sp > 0) CK(h, cudaStreamWaitEvent(h->stream, h->ev_join, 0));
+        const int n_step_parts = h->n_ctas + h->n_ctas_sp;
         if (h->n_list > 0)
-            CK(h, launch_special_list(L, h->storage, h->n_list_blocks, ds ? h->d_diag_part + 2 * h->n_ctas : nullptr,
+            CK(h, launch_special_list(L, h->storage, h->n_list_blocks, ds ? h->d_diag_part + 2 * n_step_parts : nullptr,
                                       h->stream));
         if (nb > 0) CK(h, launch_wall(L, h->storage, nb + (fs ? nbf : 0), h->stream));
         if (h->ps_start >= 0 && it >= h->ps_start && it <= h->ps_end) {
@@ -279,7 +309,7 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
         }
         if (ds) {
             const int64_t slot = h->diag_count % kRing;
-            CK(h, launch_diag_finalize(h->d_diag_part, h->n_ctas + (h->n_list > 0 ? h->n_list_blocks : 0),
+            CK(h, launch_diag_finalize(h->d_diag_part, n_step_parts + (h->n_list > 0 ? h->n_list_blocks : 0),
                                        h->d_diag_ring + slot * 2, h->stream));
             h->diag_steps[slot] = it;
             ++h->diag_count;
@@ -465,6 +495,9 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     }
     CK(h.get(), cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
     h->stream = h->own_stream;
+    CK(h.get(), cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking));
+    CK(h.get(), cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    CK(h.get(), cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
 
     // geometry on the host
     const std::string ge = classify(h->d, h->geo);
@@ -613,11 +646,11 @@ int mrlbm_get_info(const mrlbm_handle *h, mrlbm_info *info) {
     info->step = h->step;
     info->storage = h->storage;
     info->bytes_per_value = h->vbytes;
-    info->n_active_items = h->n_items;
+    info->n_active_items = h->n_items + h->n_items_sp;
     info->tile[0] = TILE_X;
     info->tile[1] = h->tile_y;
     info->tile[2] = h->lz;
-    info->reserved[0] = h->n_ctas;
+    info->reserved[0] = h->n_ctas + h->n_ctas_sp;
     info->reserved[1] = h->n_special;
     info->reserved[2] = (int32_t)std::min<int64_t>(h->n_fluid, INT32_MAX);
     return MRLBM_OK;
@@ -908,7 +941,8 @@ void batch_free_graphs(mrlbm_batch *b) {
 void batch_free_tables(mrlbm_batch *b) {
     batch_free_graphs(b);
     for (void **p : {(void **)&b->d_cases, (void **)&b->d_items, (void **)&b->d_list_blocks,
-                     (void **)&b->d_wall_blocks, (void **)&b->d_ring, (void **)&b->d_slot, (void **)&b->d_ba}) {
+                     (void **)&b->d_wall_blocks, (void **)&b->d_ring, (void **)&b->d_slot, (void **)&b->d_ba,
+                     (void **)&b->d_ba_sp}) {
         if (*p) cudaFree(*p);
         *p = nullptr;
     }
@@ -927,13 +961,14 @@ int batch_set_tiling(mrlbm_batch *b, int ty, int lz) {
     const int n = (int)b->h.size();
     std::vector<const StepArgs *> cases(n);
     std::vector<double *> ring(n);
-    std::vector<int2> items;
+    std::vector<int2> items, items_sp;
     std::vector<int4> lblocks, wblocks;
     for (int c = 0; c < n; ++c) {
         mrlbm_handle *h = b->h[c];
         cases[c] = h->d_args;
         ring[c] = h->d_force_ring;
         for (int32_t it : h->h_items) items.push_back(make_int2(c, it));
+        for (int32_t it : h->h_items_sp) items_sp.push_back(make_int2(c, it));
         if (h->n_list > 0) {
             const int first = (int)lblocks.size();
             for (int k = 0; k < h->n_list_blocks; ++k) lblocks.push_back(make_int4(c, first, h->n_list_blocks, 0));
@@ -946,11 +981,14 @@ int batch_set_tiling(mrlbm_batch *b, int ty, int lz) {
         }
     }
     b->n_items = (int)items.size();
+    b->n_items_sp = (int)items_sp.size();
+    items.insert(items.end(), items_sp.begin(), items_sp.end());
     b->n_list_blocks = (int)lblocks.size();
     b->n_wall_blocks = (int)wblocks.size();
     int per_sm = step_kernel_max_ctas_per_sm(b->storage, ty);
     if (per_sm <= 0) per_sm = 1;
-    b->n_ctas = std::max(1, std::min(b->n_items, per_sm * b->h[0]->n_sm));
+    b->n_ctas = b->n_items ? std::max(1, std::min(b->n_items, per_sm * b->h[0]->n_sm)) : 0;
+    b->n_ctas_sp = b->n_items_sp ? std::max(1, std::min(b->n_items_sp, per_sm * b->h[0]->n_sm)) : 0;
     auto up = [&](auto **dptr, const auto &v) -> cudaError_t {
         using T = typename std::remove_reference<decltype(v)>::type::value_type;
         if (v.empty()) return cudaSuccess;
@@ -975,13 +1013,25 @@ int batch_set_tiling(mrlbm_batch *b, int ty, int lz) {
     ba.force_slot = b->d_slot;
     BCK(cudaMalloc((void **)&b->d_ba, sizeof(BatchArgs)));
     BCK(cudaMemcpy(b->d_ba, &ba, sizeof(BatchArgs), cudaMemcpyHostToDevice));
-    BCK(prepare_step_batch(b->storage, ty));
+    BatchArgs bsp = ba;
+    bsp.items = b->d_items ? b->d_items + b->n_items : nullptr;
+    bsp.n_items = b->n_items_sp;
+    BCK(cudaMalloc((void **)&b->d_ba_sp, sizeof(BatchArgs)));
+    BCK(cudaMemcpy(b->d_ba_sp, &bsp, sizeof(BatchArgs), cudaMemcpyHostToDevice));
+    BCK(prepare_step_batch(b->storage, ty));  // both variants, before any capture
     return MRLBM_OK;
 }
 
 // The three batched launches of one step.
 int batch_launch(mrlbm_batch *b, int parity, int force) {
-    BCK(launch_step_batch(b->d_ba, parity, b->storage, b->tile_y, b->n_ctas, b->stream));
+    if (b->n_items_sp > 0) {
+        BCK(cudaEventRecord(b->ev_fork, b->stream));
+        BCK(cudaStreamWaitEvent(b->side_stream, b->ev_fork, 0));
+        BCK(launch_step_batch(b->d_ba_sp, parity, b->storage, b->tile_y, true, b->n_ctas_sp, b->side_stream));
+        BCK(cudaEventRecord(b->ev_join, b->side_stream));
+    }
+    if (b->n_items > 0) BCK(launch_step_batch(b->d_ba, parity, b->storage, b->tile_y, false, b->n_ctas, b->stream));
+    if (b->n_items_sp > 0) BCK(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
     BCK(launch_special_list_batch(b->d_ba, parity, force, b->storage, b->n_list_blocks, b->stream));
     BCK(launch_wall_batch(b->d_ba, parity, force, b->storage, b->n_wall_blocks, b->stream));
     return MRLBM_OK;
@@ -1077,7 +1127,10 @@ int mrlbm_batch_create(const mrlbm_case_desc *descs, int32_t n, mrlbm_batch **ou
         }
     }
     b->storage = b->h[0]->storage;
-    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         cleanup();
         return bfail(MRLBM_ERR_CUDA, "cannot create the batch stream");
     }
@@ -1109,6 +1162,9 @@ int mrlbm_batch_destroy(mrlbm_batch *b) {
         mrlbm_destroy(h);
     }
     if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->side_stream) cudaStreamDestroy(b->side_stream);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
     delete b;
     return MRLBM_OK;
 }

@@ -31,6 +31,9 @@ struct mrlbm_handle {
     bool host_only = false;
     int dev = 0, n_sm = 0;
     cudaStream_t own_stream = nullptr, stream = nullptr;
+    // the boundary-tile step launch runs beside the bulk one: side stream and fork / join events
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int storage = 0, vbytes = 4;
     StorageScale sc{};
     int64_t n = 0, fs = 0;
@@ -57,8 +60,10 @@ struct mrlbm_handle {
     int64_t *d_wl[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     uint32_t *d_tag = nullptr;  // [512]: in masks then out masks
     StepArgs args{};
-    StepArgs *d_args = nullptr;
-    std::vector<int32_t> h_items;   // host copy of the work items
+    StepArgs *d_args = nullptr;     // work items of tiles without boundary nodes (bulk kernel)
+    StepArgs *d_args_sp = nullptr;  // the same with the work items of tiles holding boundary nodes
+    int n_items_sp = 0, n_ctas_sp = 0;
+    std::vector<int32_t> h_items, h_items_sp;  // host copies of the two work-item lists
     mrlbm_batch *batch = nullptr;   // owning batch, if any
     int *d_error = nullptr;
     // sampling
@@ -82,6 +87,8 @@ struct mrlbm_handle {
 struct mrlbm_batch {
     std::vector<mrlbm_handle *> h;
     cudaStream_t stream = nullptr;
+    cudaStream_t side_stream = nullptr;  // boundary-tile step launch, forked / joined by events
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int storage = 0, tile_y = 16, lz = 0;
     int parity = 0;
     int64_t step = 0;
@@ -89,12 +96,12 @@ struct mrlbm_batch {
     int64_t force_count = 0;  // sampled steps so far (the ring slot of the cases with walls)
     // device tables (BatchArgs and what it points to)
     const StepArgs **d_cases = nullptr;
-    int2 *d_items = nullptr;
+    int2 *d_items = nullptr;  // bulk work items, then the boundary-tile work items
     int4 *d_list_blocks = nullptr, *d_wall_blocks = nullptr;
     double **d_ring = nullptr;
     int *d_slot = nullptr;
-    BatchArgs *d_ba = nullptr;
-    int n_items = 0, n_ctas = 0, n_list_blocks = 0, n_wall_blocks = 0;
+    BatchArgs *d_ba = nullptr, *d_ba_sp = nullptr;  // bulk / boundary-tile items
+    int n_items = 0, n_ctas = 0, n_items_sp = 0, n_ctas_sp = 0, n_list_blocks = 0, n_wall_blocks = 0;
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [parity][force]
 };
 

@@ -94,7 +94,8 @@ inline __host__ __device__ int64_t side_index(int slot, int x, int y, int z, int
 
 // storage: 0 f32, 1 f16, 2 bf16
 cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, bool special, cudaStream_t s);
-cudaError_t launch_step_batch(const BatchArgs *ba, int parity, int storage, int tile_y, int n_ctas, cudaStream_t s);
+cudaError_t launch_step_batch(const BatchArgs *ba, int parity, int storage, int tile_y, bool special, int n_ctas,
+                              cudaStream_t s);
 cudaError_t prepare_step_batch(int storage, int tile_y);  // before capturing batched launches
 cudaError_t launch_special_list_batch(const BatchArgs *ba, int parity, int force, int storage, int n_blocks,
                                       cudaStream_t s);

@@ -544,12 +544,18 @@ cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, bool speci
     }
 }
 
+template <typename S, int TY>
+cudaError_t prepare_ty() {
+    const cudaError_t e = configure_t<S, TY, true, true>();
+    return e != cudaSuccess ? e : configure_t<S, TY, false, true>();
+}
+
 template <typename S>
 cudaError_t prepare_s(int tile_y) {
     switch (tile_y) {
-        case 4: return configure_t<S, 4, true, true>();
-        case 8: return configure_t<S, 8, true, true>();
-        case 16: return configure_t<S, 16, true, true>();
+        case 4: return prepare_ty<S, 4>();
+        case 8: return prepare_ty<S, 8>();
+        case 16: return prepare_ty<S, 16>();
         default: return cudaErrorInvalidValue;
     }
 }
@@ -563,12 +569,18 @@ cudaError_t prepare_step_batch(int storage, int tile_y) {
     }
 }
 
-cudaError_t launch_step_batch(const BatchArgs *ba, int parity, int storage, int tile_y, int n_ctas, cudaStream_t s) {
+cudaError_t launch_step_batch(const BatchArgs *ba, int parity, int storage, int tile_y, bool special, int n_ctas,
+                              cudaStream_t s) {
     switch (storage) {
-        case MRLBM_STORAGE_F32: return launch_s<float, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
-        case MRLBM_STORAGE_F16: return launch_s<__half, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
+        case MRLBM_STORAGE_F32:
+            return special ? launch_s<float, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s)
+                           : launch_s<float, false, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
+        case MRLBM_STORAGE_F16:
+            return special ? launch_s<__half, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s)
+                           : launch_s<__half, false, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
         case MRLBM_STORAGE_BF16:
-            return launch_s<__nv_bfloat16, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
+            return special ? launch_s<__nv_bfloat16, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s)
+                           : launch_s<__nv_bfloat16, false, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
         default: return cudaErrorInvalidValue;
     }
 }
