@@ -235,6 +235,9 @@ int setup_tiling(mrlbm_handle *h, int ty, int lz) {
         if (h->n_list_pop > 0) CK(h, cudaMalloc((void **)&h->d_popbuf, (size_t)h->n_list_pop * 27 * sizeof(float)));
     }
     StepArgs &a = h->args;
+    // a single case's items are uniform: CTAs stride through them, which keeps neighbouring
+    // tiles in flight together (L2 reuse of the rim columns); batches claim items on demand
+    a.work_counter = nullptr;
     a.items = h->d_items;
     a.n_items = h->n_items;
     a.tile_slot = h->d_tile_slot;
@@ -253,6 +256,7 @@ int setup_tiling(mrlbm_handle *h, int ty, int lz) {
     StepArgs asp = a;
     asp.items = h->d_items ? h->d_items + h->n_items : nullptr;
     asp.n_items = h->n_items_sp;
+    asp.work_counter = nullptr;
     if (!h->d_args_sp) CK(h, cudaMalloc((void **)&h->d_args_sp, sizeof(StepArgs)));
     CK(h, cudaMemcpy(h->d_args_sp, &asp, sizeof(StepArgs), cudaMemcpyHostToDevice));
     return MRLBM_OK;
@@ -942,7 +946,7 @@ void batch_free_tables(mrlbm_batch *b) {
     batch_free_graphs(b);
     for (void **p : {(void **)&b->d_cases, (void **)&b->d_items, (void **)&b->d_list_blocks,
                      (void **)&b->d_wall_blocks, (void **)&b->d_ring, (void **)&b->d_slot, (void **)&b->d_ba,
-                     (void **)&b->d_ba_sp}) {
+                     (void **)&b->d_ba_sp, (void **)&b->d_work}) {
         if (*p) cudaFree(*p);
         *p = nullptr;
     }
@@ -1003,7 +1007,10 @@ int batch_set_tiling(mrlbm_batch *b, int ty, int lz) {
     BCK(up(&b->d_wall_blocks, wblocks));
     BCK(cudaMalloc((void **)&b->d_slot, sizeof(int)));
     BCK(cudaMemset(b->d_slot, 0, sizeof(int)));
+    BCK(cudaMalloc((void **)&b->d_work, 2 * sizeof(int)));
+    BCK(cudaMemset(b->d_work, 0, 2 * sizeof(int)));
     BatchArgs ba;
+    ba.work_counter = b->d_work;
     ba.cases = b->d_cases;
     ba.items = b->d_items;
     ba.n_items = b->n_items;
@@ -1016,6 +1023,7 @@ int batch_set_tiling(mrlbm_batch *b, int ty, int lz) {
     BatchArgs bsp = ba;
     bsp.items = b->d_items ? b->d_items + b->n_items : nullptr;
     bsp.n_items = b->n_items_sp;
+    bsp.work_counter = b->d_work + 1;
     BCK(cudaMalloc((void **)&b->d_ba_sp, sizeof(BatchArgs)));
     BCK(cudaMemcpy(b->d_ba_sp, &bsp, sizeof(BatchArgs), cudaMemcpyHostToDevice));
     BCK(prepare_step_batch(b->storage, ty));  // both variants, before any capture
@@ -1024,6 +1032,7 @@ int batch_set_tiling(mrlbm_batch *b, int ty, int lz) {
 
 // The three batched launches of one step.
 int batch_launch(mrlbm_batch *b, int parity, int force) {
+    BCK(cudaMemsetAsync(b->d_work, 0, 2 * sizeof(int), b->stream));
     if (b->n_items_sp > 0) {
         BCK(cudaEventRecord(b->ev_fork, b->stream));
         BCK(cudaStreamWaitEvent(b->side_stream, b->ev_fork, 0));

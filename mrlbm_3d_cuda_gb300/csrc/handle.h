@@ -102,6 +102,7 @@ struct mrlbm_batch {
     int *d_slot = nullptr;
     BatchArgs *d_ba = nullptr, *d_ba_sp = nullptr;  // bulk / boundary-tile items
     int n_items = 0, n_ctas = 0, n_items_sp = 0, n_ctas_sp = 0, n_list_blocks = 0, n_wall_blocks = 0;
+    int *d_work = nullptr;  // [2] work-item counters of the two batched step launches
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [parity][force]
 };
 

@@ -62,6 +62,7 @@ struct StepArgs {
     int n_list_pop = 0, n_list = 0;
     float *popbuf = nullptr;              // [27][n_list_pop]
     const int32_t *row_base = nullptr;    // [slot][z][tile row]: first list entry of the row
+    int *work_counter = nullptr;          // work items claimed beyond the first gridDim.x (zeroed per launch)
 };
 
 // Several independent cases advanced together: one step-kernel launch over the work items of
@@ -75,6 +76,7 @@ struct BatchArgs {
     const int4 *wall_blocks = nullptr;       // per wall block: {case, first block of the case, blocks, 0}
     double *const *force_ring = nullptr;     // per case: force ring of the case
     const int *force_slot = nullptr;         // ring slot of the sampled step
+    int *work_counter = nullptr;             // as StepArgs::work_counter, for the batched launch
 };
 
 // Per-step launch parameters.
@@ -145,11 +147,13 @@ cudaError_t launch_surface_pressure(const StepArgs *ga, int buf, int storage, in
 //   [0, 1536)            StepArgs
 //   [1536, 1552)         mass / energy sums (2 doubles)
 //   [1600, 1604)         error word
+//   [1604, 1608)         work-item counter of the step kernel
 //   [2048, 18432)        per-CTA diagnostics partials, 2 doubles per CTA
 //   [18432, 65536)       work items, one int32 each
 constexpr int kNoAllocScratchBytes = 64 * 1024;
 constexpr int kNoAllocDiagOffset = 1536;
 constexpr int kNoAllocErrorOffset = 1600;
+constexpr int kNoAllocWorkOffset = 1604;
 constexpr int kNoAllocPartOffset = 2048;
 constexpr int kNoAllocMaxCtas = 1024;
 constexpr int kNoAllocItemsOffset = kNoAllocPartOffset + kNoAllocMaxCtas * 2 * (int)sizeof(double);

@@ -262,7 +262,12 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     float *const dn_base = smem + (G::NUP + G::NFL) * G::PLANE;
     double dmD = 0.0, deD = 0.0;
 
-    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    // Work items: the first gridDim.x go by block index, the rest are claimed on demand from
+    // a counter zeroed before every launch, so CTAs that finish early take more (no static
+    // last-wave imbalance).  Without a counter the CTAs stride through the list.
+    int *const work = BATCH ? ba->work_counter : ga->work_counter;
+    __shared__ int s_next;
+    for (int it = blockIdx.x; it < n_items;) {
         int item;
         if constexpr (BATCH) {
             const int2 e = ba->items[it];
@@ -422,7 +427,9 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 if (k + 1 <= last) rim_plane(k + 1, pb, pa);
             }
         }
+        if (tid == 0) s_next = work ? (int)gridDim.x + atomicAdd(work, 1) : it + (int)gridDim.x;
         __syncthreads();  // the next item reuses the rings from slot 0
+        it = s_next;
     }
 
     if (diag) {
@@ -632,6 +639,7 @@ __global__ void noalloc_setup_kernel(const StepArgs a, unsigned char *scratch, i
     if (i == 0) {
         *(StepArgs *)scratch = a;
         *(int *)(scratch + kNoAllocErrorOffset) = 0;
+        *(int *)(scratch + kNoAllocWorkOffset) = 0;
     }
     int32_t *items = (int32_t *)(scratch + kNoAllocItemsOffset);
     for (int j = i; j < n_items; j += gridDim.x * blockDim.x) items[j] = (j % tiles) | ((j / tiles) << 20);
@@ -741,6 +749,7 @@ int noalloc_periodic_step(const NoAllocStep &p, std::string &err) {
     sa.rho0 = p.rho0;
     for (int k = 0; k < 3; ++k) sa.sc.s[k] = sa.sc.is[k] = 1.f;
     sa.error = (int *)(scratch + kNoAllocErrorOffset);
+    sa.work_counter = (int *)(scratch + kNoAllocWorkOffset);
 
     noalloc_setup_kernel<<<(n_items + 255) / 256, 256, 0, p.stream>>>(sa, scratch, tiles, n_items);
     if ((e = cudaGetLastError()) != cudaSuccess) return noalloc_cuda_fail(e, "set-up launch", err);
