@@ -97,6 +97,8 @@ extern "C" {
 #define MRLBM_BND_FLUID_LIST 6  /* int64  [NB_FLUID] BCFLUID node index                       */
 #define MRLBM_BND_TAG_IN_MASK 7 /* uint32 [256] d_incomingMask_bcfluid (cylinder_helpers.cuh:230-299) */
 #define MRLBM_BND_TAG_OUT_MASK 8 /* uint32 [256] d_outgoingMask_bcfluid                       */
+#define MRLBM_BND_SOLID_LIST 9  /* int64  [NB_SOLID] BCSOLID node index (z walls only,     
+                                   cylinder_helpers.cuh:49-114 bcsolidList)                  */
 
 /* ---- case descriptor -------------------------------------------------------------------
  * A runtime POD replacing the reference's per-case constexpr headers.  Fill it with
@@ -141,7 +143,8 @@ typedef struct mrlbm_info {
     int32_t bytes_per_value;
     int32_t n_active_items;  /* work items (tile column x z-segment) the step kernel visits */
     int32_t tile[3];      /* tile x, tile y, z-segment length used by the step kernel     */
-    int32_t reserved[8];
+    int32_t nb_solid[2];  /* BCSOLID nodes per wall (z walls only)                       */
+    int32_t reserved[6];
 } mrlbm_info;
 
 typedef struct mrlbm_handle mrlbm_handle;

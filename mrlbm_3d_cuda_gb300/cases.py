@@ -15,12 +15,15 @@ def _finish(d: N.CaseDesc, storage: int = N.STORAGE_F32) -> N.CaseDesc:
     return N.finalize(d)
 
 
-def reference_cylinder(storage: int = N.STORAGE_F32, diameter: int = 16) -> N.CaseDesc:
+def reference_cylinder(storage: int = N.STORAGE_F32, diameter: int = 16, *, periodic_z: bool = True) -> N.CaseDesc:
     """The reference's shipped cylinder case (cases/cylinder/constants.cuh:8-54):
     336 x 144 x 48, D = 16 at (71.5, 71.5), Re = 100, U = 0.1, periodic y and z, convective outlet.
     `diameter` rescales it as the reference's constants do when D is edited: LW = LN = LS = 4D,
-    LE = 16D, NZ = 3D, centre LW + (D - 1) / 2, classification box +-4 nodes around the body."""
+    LE = 16D, NZ = 3D, centre LW + (D - 1) / 2, classification box +-4 nodes around the body.
+    `periodic_z=False` is the reference built with Z_PERIODIC 0 (constants.cuh:10): no-slip
+    z = 0 / NZ-1 faces, with BCSOLID nodes where they meet the body."""
     d = N.default_desc(N.GEOM_CYLINDER)
+    d.periodic[2] = int(periodic_z)
     if diameter != 16:
         D = int(diameter)
         lw, le, ln = 4 * D, 16 * D, 4 * D
@@ -41,14 +44,16 @@ def reference_annulus(storage: int = N.STORAGE_F32) -> N.CaseDesc:
 
 def cylinder_channel(nx: int, ny: int, nz: int, d: float, xc: float, yc: float, u: float, re: float, *,
                      lw: int | None = None, ls: int | None = None, periodic_y: bool = False,
-                     convective: bool = False, storage: int = N.STORAGE_F32, triangular: bool = True) -> N.CaseDesc:
+                     periodic_z: bool = True, convective: bool = False, storage: int = N.STORAGE_F32,
+                     triangular: bool = True) -> N.CaseDesc:
     """Flow past a circular cylinder (axis z) in a channel: velocity inlet at x = 0,
-    zero-gradient (or convective) outlet at x = nx-1, no-slip or periodic y, periodic z.
+    zero-gradient (or convective) outlet at x = nx-1, no-slip or periodic y, periodic or
+    no-slip z (z walls add BCSOLID nodes where the z faces meet the body).
     `lw`, `ls` set the reference's classification window (LW-4 .. LW+D+4); by default it is
     centred on the cylinder."""
     desc = N.default_desc(N.GEOM_CYLINDER)
     desc.nx, desc.ny, desc.nz = nx, ny, nz
-    desc.periodic[0], desc.periodic[1], desc.periodic[2] = 0, int(periodic_y), 1
+    desc.periodic[0], desc.periodic[1], desc.periodic[2] = 0, int(periodic_y), int(periodic_z)
     desc.d_wall[0] = float(d)
     desc.xc, desc.yc = float(xc), float(yc)
     desc.u_max, desc.re = float(u), float(re)
@@ -66,12 +71,12 @@ def cylinder_channel(nx: int, ny: int, nz: int, d: float, xc: float, yc: float, 
 
 def annulus(nx: int, ny: int, nz: int, r_in: float, r_out: float, u_inner: float, re: float, *,
             u_outer: float = 0.0, xc: float | None = None, yc: float | None = None,
-            storage: int = N.STORAGE_F32) -> N.CaseDesc:
+            periodic_z: bool = True, storage: int = N.STORAGE_F32) -> N.CaseDesc:
     """Taylor-Couette annulus: concentric walls (axis z), wall speeds tangential in the
-    rotated frame, Re on the gap width, periodic z."""
+    rotated frame, Re on the gap width, periodic or no-slip z (BCSOLID nodes on both walls)."""
     desc = N.default_desc(N.GEOM_ANNULUS)
     desc.nx, desc.ny, desc.nz = nx, ny, nz
-    desc.periodic[0], desc.periodic[1], desc.periodic[2] = 0, 0, 1
+    desc.periodic[0], desc.periodic[1], desc.periodic[2] = 0, 0, int(periodic_z)
     desc.d_wall[0], desc.d_wall[1] = 2.0 * r_in, 2.0 * r_out
     desc.xc = 0.5 * (nx - 1) if xc is None else xc
     desc.yc = 0.5 * (ny - 1) if yc is None else yc

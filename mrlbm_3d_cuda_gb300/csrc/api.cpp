@@ -644,6 +644,7 @@ int mrlbm_get_info(const mrlbm_handle *h, mrlbm_info *info) {
     for (int w = 0; w < 2; ++w) {
         info->nb[w] = (int32_t)h->geo.wall[w].list.size();
         info->nb_fluid[w] = (int32_t)h->geo.wall[w].fluid_list.size();
+        info->nb_solid[w] = (int32_t)h->geo.wall[w].solid_list.size();
     }
     info->omega = h->der.omega;
     info->tau = h->der.tau;
@@ -841,6 +842,7 @@ int mrlbm_get_boundary(mrlbm_handle *h, int32_t wall, int32_t what, int32_t layo
         case MRLBM_BND_FLUID_LIST: return copy_list(wd.fluid_list);
         case MRLBM_BND_TAG_IN_MASK: return copy_u(h->geo.tag_in_mask, 256);
         case MRLBM_BND_TAG_OUT_MASK: return copy_u(h->geo.tag_out_mask, 256);
+        case MRLBM_BND_SOLID_LIST: return copy_list(wd.solid_list);
         default: return fail(h, MRLBM_ERR_INVALID_ARG, "bad boundary array id");
     }
 }

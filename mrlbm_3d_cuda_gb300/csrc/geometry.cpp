@@ -6,6 +6,7 @@
 //   mark_*_solid                   cases/cylinder/nodeClass.cuh:110-125, cases/annulus/nodeClass.cuh:109-126
 //   classify_boundary_nodes_*      cases/cylinder/nodeClass.cuh:138-216, cases/annulus/nodeClass.cuh:139-257
 //   classify_bcfluid_nodes_*       cases/cylinder/nodeClass.cuh:218-252, cases/annulus/nodeClass.cuh:259-307
+//   classify_bcsolid_nodes_*       cases/cylinder/nodeClass.cuh:254-287, cases/annulus/nodeClass.cuh:309-357
 //   buildBoundaryList / assignBoundaryIndices  cases/cylinder/cylinder_helpers.cuh:49-132
 //   compute_unit_vectors_boundary_nodes        cases/cylinder/cylinder_helpers.cuh:10-47
 //   find_incomings_outgoings                   cases/cylinder/cylinder_helpers.cuh:134-228
@@ -200,9 +201,23 @@ std::string classify(const mrlbm_case_desc &d, Geometry &g) {
                     g.payload[i] = tag;
                 }
     }
+    // 4b. BCSOLID (z walls only): plain z-face nodes whose neighbours hold bulk fluid in fewer
+    //     than four octants, tagged by those octants (nodeClass.cuh:254-287 scans the
+    //     cylinder's window, annulus/nodeClass.cuh:309-357 the whole plane, like scan_box)
     if (!d.periodic[2] && d.triangular) {
-        // BCSOLID nodes (non-periodic z) are not built: cases/cylinder/boundaries.cuh:1039-1214.
-        return "non-periodic z with curved walls (BCSOLID nodes) is not supported";
+        for (int z : {0, d.nz - 1})
+            for (int y = by0; y < by1; ++y)
+                for (int x = bx0; x < bx1; ++x) {
+                    s.neighbours(x, y, z, nb);
+                    if (nb[0] != C_BACK && nb[0] != C_FRONT) continue;
+                    if (Scan::octant_bits(nb, C_BULK, bits) >= 4) continue;
+                    uint32_t tag = 0;
+                    for (int b = 0; b < 8; ++b) tag |= (uint32_t)bits[b] << b;
+                    const bool outer = annulus && !(s.radius(x, y) < r_mid);
+                    const int64_t i = s.idx(x, y, z);
+                    g.cls[i] = outer ? C_BCSOLID_OUTER : C_BCSOLID_INNER;
+                    g.payload[i] = tag;
+                }
     }
 
     // 5. lists in lexicographic z, y, x scan order; wall index into the payload
@@ -215,6 +230,8 @@ std::string classify(const mrlbm_case_desc &d, Geometry &g) {
                     case C_OUTER: g.wall[1].list.push_back(i); break;
                     case C_BCFLUID_INNER: g.wall[0].fluid_list.push_back(i); break;
                     case C_BCFLUID_OUTER: g.wall[1].fluid_list.push_back(i); break;
+                    case C_BCSOLID_INNER: g.wall[0].solid_list.push_back(i); break;
+                    case C_BCSOLID_OUTER: g.wall[1].solid_list.push_back(i); break;
                     default: break;
                 }
             }

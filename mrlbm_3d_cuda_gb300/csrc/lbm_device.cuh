@@ -378,6 +378,46 @@ __device__ __forceinline__ bool bcfluid_closure(uint32_t tag, uint32_t mask, con
     return true;
 }
 
+// BCSOLID closure (z walls only) of a z-face node beside the body, tagged by the octants of its
+// neighbourhood that hold bulk fluid.  The eight tags with three of the four in-domain octants
+// (0x0F or 0xF0 less one bit) have a closure; the missing octant (ox, oy, oz) points into the
+// body.  The known populations are the ones pulled from inside the domain (cz != oz) less the
+// two sourced from the body, x + (ox, oy, 0) and x + (ox, oy, oz).  The node is held at rest
+// (u = 0, mxx = myy = mzz = mxy = 0); rho, mxz and myz follow from rhoI and the incoming mxz,
+// myz.  cases/cylinder/boundaries.cuh:1039-1214 spells this out as one case per tag; here the
+// eight cases are one formula in px = ox oz and py = oy oz.  Returns false for other tags
+// (the moments stay pre-stream).
+__device__ __forceinline__ bool bcsolid_closure(uint32_t tag, const float f[27], float omega, Mom &o) {
+    int miss;
+    if ((tag & 0xF0u) == 0u && __popc(tag ^ 0x0Fu) == 1) miss = __ffs(tag ^ 0x0Fu) - 1;
+    else if ((tag & 0x0Fu) == 0u && __popc(tag ^ 0xF0u) == 1) miss = __ffs(tag ^ 0xF0u) - 1;
+    else return false;
+    const int ox = (miss & 1) ? 1 : -1, oy = (miss & 2) ? 1 : -1, oz = (miss & 4) ? 1 : -1;
+    float rI = 0.f, sxz = 0.f, syz = 0.f;
+#pragma unroll
+    for (int q = 0; q < 27; ++q) {
+        const int cx = cxq(q), cy = cyq(q), cz = czq(q);
+        if (cz == oz || (cx == -ox && cy == -oy)) continue;
+        const float v = f[q];
+        rI += v;
+        if (cx * cz > 0) sxz += v;
+        else if (cx * cz < 0) sxz -= v;
+        if (cy * cz > 0) syz += v;
+        else if (cy * cz < 0) syz -= v;
+    }
+    const float inv = (float)(1.0 / (double)rI);
+    const float mxzI = sxz * inv, myzI = syz * inv;
+    const float px = (float)(ox * oz), py = (float)(oy * oz), pxy = px * py;
+    const float w1 = omega - 1.0f;
+    const float r = (108.0f * (10.0f - w1 * (px * mxzI) - w1 * (py * myzI)) * rI) / (874.0f + omega);
+    o.rho = r;
+    o.ux = o.uy = o.uz = 0.0f;
+    o.mxx = o.myy = o.mzz = o.mxy = 0.0f;
+    o.mxz = (198.0f * mxzI * rI + (18.0f * pxy) * myzI * rI + px * r) / (90.0f * r);
+    o.myz = ((18.0f * pxy) * mxzI * rI + 198.0f * myzI * rI + py * r) / (90.0f * r);
+    return true;
+}
+
 // Incoming rho and second moments at a curved-wall node in the frame rotated to its
 // normal (cos = nx, sin = ny); u is left to the wall kernel.
 __device__ __forceinline__ void incoming_rotated(float nx, float ny, uint32_t mask, const float f[27], Mom &o) {

@@ -46,13 +46,14 @@ struct WallData {
     std::vector<float> nx, ny, delta;
     std::vector<uint32_t> in_mask, out_mask;
     std::vector<int64_t> fluid_list; // BCFLUID nodes of this wall, scan order
+    std::vector<int64_t> solid_list; // BCSOLID nodes of this wall (z walls only), scan order
 };
 
 // Result of the host classification (lexicographic node order idx = x + nx*(y + ny*z)).
 struct Geometry {
     int nx = 0, ny = 0, nz = 0;
     std::vector<uint8_t> cls;       // NodeClass per node
-    std::vector<uint32_t> payload;  // boundary index or BCFLUID tag
+    std::vector<uint32_t> payload;  // boundary index or BCFLUID / BCSOLID tag
     std::vector<uint8_t> frozen;    // node of an all-solid reference block column
     std::vector<uint8_t> stencil;   // needs its post-stream moments kept for the wall kernel
     WallData wall[2];

@@ -12,8 +12,9 @@
 //   cylinder_boundary_moments / annulus_boundary_moments
 //                                       MRLBM_3D/src/cases/cylinder/cylinder_kernels.cuh:32-65,
 //                                       MRLBM_3D/src/cases/annulus/annulus_kernels.cuh:17-58
-//   boundary_condition (faces, edges, corners), fluid_boundary_condition (BCFLUID)
-//                                       MRLBM_3D/src/cases/cylinder/boundaries.cuh:8-1037
+//   boundary_condition (faces, edges, corners), fluid_boundary_condition (BCFLUID),
+//   bcsolid_boundary_condition (BCSOLID, z walls only)
+//                                       MRLBM_3D/src/cases/cylinder/boundaries.cuh:8-1214
 //   evaluate_incoming_moments_rotated   MRLBM_3D/src/boundary/curvedLBM.cu:5-59
 //   moment_collision                    MRLBM_3D/src/solver/mlbm.cu:3-16
 //   compute_force_mass_kernel (BCFLUID part)  MRLBM_3D/src/statistics/forces.cu:25-133
@@ -86,6 +87,10 @@ __device__ __forceinline__ int special_node(const StepArgs &a, int parity, bool 
             const uint32_t tag = (w >> NW_PAYLOAD_SHIFT) & 0xFFu;
             Mom o = prev;
             if (bcfluid_closure(tag, a.tag_in[tag], fl, a.bcf_strong, a.omega, o)) m = o;
+        } else if (cls == C_BCSOLID_INNER || cls == C_BCSOLID_OUTER) {
+            const uint32_t tag = (w >> NW_PAYLOAD_SHIFT) & 0xFFu;
+            Mom o = prev;
+            if (bcsolid_closure(tag, fl, a.omega, o)) m = o;
         } else {
             PlanarCtx c;
             c.omega = a.omega;

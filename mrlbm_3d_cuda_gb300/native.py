@@ -24,10 +24,13 @@ STORAGE_F32, STORAGE_F16, STORAGE_BF16 = 0, 1, 2
 MASS_EQUILIBRIUM, MASS_STRONG = 0, 1
 INIT_REFERENCE_NOISE, INIT_REST, INIT_TAYLOR_GREEN, INIT_UNIFORM, INIT_NOISY_UNIFORM = 0, 1, 2, 3, 4
 LAYOUT_LEXICOGRAPHIC, LAYOUT_REF_TILED = 0, 1
+# node classes in the high bits of a node type (common/nodeTypeMap.cuh:39-80 order)
+NODE_BULK, NODE_SOLID, NODE_INNER, NODE_OUTER, NODE_BCFLUID_INNER, NODE_BCFLUID_OUTER, NODE_BCSOLID_INNER, \
+    NODE_BCSOLID_OUTER, NODE_NORTH, NODE_SOUTH, NODE_EAST, NODE_WEST, NODE_FRONT, NODE_BACK = range(14)
 FIELDS = ("rho", "ux", "uy", "uz", "mxx", "myy", "mzz", "mxy", "mxz", "myz")
 FIELD_ALL = 0x3FF
 BND_LIST, BND_NORMAL_X, BND_NORMAL_Y, BND_DELTA, BND_IN_MASK, BND_OUT_MASK, BND_FLUID_LIST, BND_TAG_IN_MASK, \
-    BND_TAG_OUT_MASK = range(9)
+    BND_TAG_OUT_MASK, BND_SOLID_LIST = range(10)
 
 
 class CaseDesc(C.Structure):
@@ -61,7 +64,8 @@ class Info(C.Structure):
         ("storage", C.c_int32), ("bytes_per_value", C.c_int32),
         ("n_active_items", C.c_int32),
         ("tile", C.c_int32 * 3),
-        ("reserved", C.c_int32 * 8),
+        ("nb_solid", C.c_int32 * 2),
+        ("reserved", C.c_int32 * 6),
     ]
 
 

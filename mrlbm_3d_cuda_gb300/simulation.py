@@ -145,16 +145,18 @@ class Simulation:
         return out
 
     def boundary(self, wall: int = 0, layout: int = N.LAYOUT_LEXICOGRAPHIC) -> dict:
-        """Boundary arrays of a curved wall: lists, normals, wall distances, direction masks."""
+        """Boundary arrays of a curved wall: lists, normals, wall distances, direction masks,
+        BCFLUID and BCSOLID node lists."""
         nb = int(self.info.nb[wall])
         nbf = int(self.info.nb_fluid[wall])
+        nbs = int(self.info.nb_solid[wall])
         L = N.lib()
         res = {}
         spec = [("list", N.BND_LIST, np.int64, nb), ("nx", N.BND_NORMAL_X, np.float32, nb),
                 ("ny", N.BND_NORMAL_Y, np.float32, nb), ("delta", N.BND_DELTA, np.float32, nb),
                 ("in_mask", N.BND_IN_MASK, np.uint32, nb), ("out_mask", N.BND_OUT_MASK, np.uint32, nb),
                 ("fluid_list", N.BND_FLUID_LIST, np.int64, nbf), ("tag_in_mask", N.BND_TAG_IN_MASK, np.uint32, 256),
-                ("tag_out_mask", N.BND_TAG_OUT_MASK, np.uint32, 256)]
+                ("tag_out_mask", N.BND_TAG_OUT_MASK, np.uint32, 256), ("solid_list", N.BND_SOLID_LIST, np.int64, nbs)]
         for name, what, dt, n in spec:
             a = np.zeros(max(n, 1), dtype=dt)
             self._ck(L.mrlbm_get_boundary(self._h, wall, what, layout, a.ctypes.data_as(C.c_void_p), a.size))

@@ -99,10 +99,11 @@ class Oracle:
         L = lib()
         nb = L.oracle_wall_size(self._p, wall, 0)
         nbf = L.oracle_wall_size(self._p, wall, 1)
+        nbs = L.oracle_wall_size(self._p, wall, 2)
         spec = [("list", 0, np.int64, nb), ("nx", 1, np.float32, nb), ("ny", 2, np.float32, nb),
                 ("delta", 3, np.float32, nb), ("in_mask", 4, np.uint32, nb), ("out_mask", 5, np.uint32, nb),
                 ("fluid_list", 6, np.int64, nbf), ("tag_in_mask", 7, np.uint32, 256),
-                ("tag_out_mask", 8, np.uint32, 256)]
+                ("tag_out_mask", 8, np.uint32, 256), ("solid_list", 9, np.int64, nbs)]
         res = {}
         for name, what, dt, n in spec:
             a = np.zeros(max(n, 1), dtype=dt)

@@ -16,6 +16,7 @@
 //   step order                MRLBM_3D/src/main.cu:21-35
 //   planar closures           MRLBM_3D/src/cases/cylinder/boundaries.cuh:8-843
 //   BCFLUID closure           MRLBM_3D/src/cases/cylinder/boundaries.cuh:845-1037
+//   BCSOLID closure           MRLBM_3D/src/cases/cylinder/boundaries.cuh:1039-1214 (z walls only)
 //   curved-wall closure       MRLBM_3D/src/boundary/curvedLBM.cu:5-132, extrapolation_utils.cuh:5-107,
 //                             numerical_solution.cu:4-279
 //   forces                    MRLBM_3D/src/statistics/forces.cu:3-133
@@ -160,7 +161,7 @@ void collide(T omega, M10<T> &m) {
 }
 
 struct WallO {
-    std::vector<int64_t> list, fluid;
+    std::vector<int64_t> list, fluid, solid;
     std::vector<float> nx, ny, delta;
     std::vector<uint32_t> in, out;
 };
@@ -310,13 +311,27 @@ struct Oracle {
                             const uint32_t c = (n_walls == 2 && !(radius(x, y) < RMID)) ? BCF_OUT : BCF_IN;
                             type[idx(x, y, z)] = (c << 20) | tag;
                         }
-            if (!d.periodic[2]) return "non-periodic z with curved walls is not restated";
+            // BCSOLID (nodeClass.cuh:254-287, annulus/nodeClass.cuh:309-357): z walls only
+            if (d.triangular && !d.periodic[2])
+                for (int z : {0, nz - 1})
+                    for (int y = d.scan_box[2]; y < d.scan_box[3]; ++y)
+                        for (int x = d.scan_box[0]; x < d.scan_box[1]; ++x) {
+                            neighbours(x, y, z, nb);
+                            if (nb[0] != BACK && nb[0] != FRONT) continue;
+                            if (bits_of(nb, BULK, bits) >= 4) continue;
+                            uint32_t tag = 0;
+                            for (int b = 0; b < 8; ++b) tag += (uint32_t)bits[b] << b;
+                            const uint32_t c = (n_walls == 2 && !(radius(x, y) < RMID)) ? BCS_OUT : BCS_IN;
+                            type[idx(x, y, z)] = (c << 20) | tag;
+                        }
             for (int64_t i = 0; i < n; ++i) {
                 const uint32_t c = cls(i);
                 if (c == INNER) wall[0].list.push_back(i);
                 else if (c == OUTER) wall[1].list.push_back(i);
                 else if (c == BCF_IN) wall[0].fluid.push_back(i);
                 else if (c == BCF_OUT) wall[1].fluid.push_back(i);
+                else if (c == BCS_IN) wall[0].solid.push_back(i);
+                else if (c == BCS_OUT) wall[1].solid.push_back(i);
             }
             for (int w = 0; w < n_walls; ++w) {
                 WallO &W = wall[w];
@@ -723,6 +738,44 @@ struct Oracle {
         }
     }
 
+    // bcsolid_boundary_condition (boundaries.cuh:1039-1214), z walls only.  Per tag: the 16
+    // populations the reference sums into rhoI, and the signs (px, py) with which its incoming
+    // mxzI, myzI enter rho, mxz and myz (TAG_BCS_1..8 = 7, 11, 13, 14, 112, 176, 208, 224).
+    void bcsolid(uint32_t tag, const T *p, M10<T> &m) const {
+        struct Row { uint32_t tag; int known[16]; int px, py; };
+        static const Row rows[8] = {
+            {7, {0, 1, 2, 3, 4, 5, 7, 9, 11, 13, 14, 16, 18, 19, 23, 25}, -1, -1},
+            {11, {0, 1, 2, 3, 4, 5, 7, 8, 9, 11, 14, 16, 18, 19, 22, 25}, 1, -1},
+            {13, {0, 1, 2, 3, 4, 5, 7, 8, 9, 11, 13, 16, 18, 19, 22, 23}, -1, 1},
+            {14, {0, 1, 2, 3, 4, 5, 8, 9, 11, 13, 14, 16, 18, 22, 23, 25}, 1, 1},
+            {112, {0, 1, 2, 3, 4, 6, 7, 10, 12, 13, 14, 15, 17, 21, 24, 26}, 1, 1},
+            {176, {0, 1, 2, 3, 4, 6, 7, 8, 10, 12, 14, 15, 17, 20, 21, 24}, -1, 1},
+            {208, {0, 1, 2, 3, 4, 6, 7, 8, 10, 12, 13, 15, 17, 20, 21, 26}, 1, -1},
+            {224, {0, 1, 2, 3, 4, 6, 8, 10, 12, 13, 14, 15, 17, 20, 24, 26}, -1, -1},
+        };
+        const Row *row = nullptr;
+        for (const Row &r : rows)
+            if (r.tag == tag) row = &r;
+        if (!row) return;  // other tags keep the pre-stream moments
+        T rI = 0, sxz = 0, syz = 0;
+        for (int k = 0; k < 16; ++k) {
+            const int q = row->known[k];
+            rI += p[q];
+            const int xz = CX[q] * CZ[q], yz = CY[q] * CZ[q];
+            if (xz > 0) sxz += p[q]; else if (xz < 0) sxz -= p[q];
+            if (yz > 0) syz += p[q]; else if (yz < 0) syz -= p[q];
+        }
+        const T iv = (T)(1.0 / (double)rI);
+        const T mxzI = sxz * iv, myzI = syz * iv;
+        const T px = (T)row->px, py = (T)row->py, O = omega;
+        const T rho = ((T)108 * ((T)10 - (O - (T)1) * (px * mxzI) - (O - (T)1) * (py * myzI)) * rI) / ((T)874 + O);
+        m.rho = rho;
+        m.ux = m.uy = m.uz = 0;
+        m.mxx = m.myy = m.mzz = m.mxy = 0;
+        m.mxz = ((T)198 * mxzI * rI + (T)18 * (px * py) * myzI * rI + px * rho) / ((T)90 * rho);
+        m.myz = ((T)18 * (px * py) * mxzI * rI + (T)198 * myzI * rI + py * rho) / ((T)90 * rho);
+    }
+
     // evaluate_incoming_moments_rotated (curvedLBM.cu:5-59)
     void incoming_rot(T c, T s, uint32_t mask, const T *p, M10<T> &m) const {
         T r = 0, a = 0, b = 0, e = 0, f = 0, g = 0, h = 0;
@@ -904,6 +957,8 @@ struct Oracle {
                 incoming_rot((T)wall[w].nx[bi], (T)wall[w].ny[bi], wall[w].in[bi], f, m);
             } else if (c == BCF_IN || c == BCF_OUT) {
                 bcfluid(type[i] & 0xFFFFFu, f, m);
+            } else if (c == BCS_IN || c == BCS_OUT) {
+                bcsolid(type[i] & 0xFFFFFu, f, m);
             } else if (c != SOLID) {
                 planar(c, i, f, m);
             }
@@ -1119,13 +1174,14 @@ void oracle_get_node_types(void *p, uint32_t *out) { DISPATCH(p, std::memcpy(out
 
 void oracle_get_frozen(void *p, uint8_t *out) { DISPATCH(p, std::memcpy(out, o->frozen.data(), o->n)); }
 
-int oracle_wall_size(void *p, int w, int fluid) {
+// kind: 0 wall nodes, 1 BCFLUID nodes, 2 BCSOLID nodes
+int oracle_wall_size(void *p, int w, int kind) {
     int r = 0;
-    DISPATCH(p, r = fluid ? (int)o->wall[w].fluid.size() : (int)o->wall[w].list.size());
+    DISPATCH(p, r = (int)(kind == 2 ? o->wall[w].solid.size() : kind == 1 ? o->wall[w].fluid.size() : o->wall[w].list.size()));
     return r;
 }
 
-// what: 0 list, 1 nx, 2 ny, 3 delta, 4 in, 5 out, 6 fluid list, 7 tag in, 8 tag out
+// what: 0 list, 1 nx, 2 ny, 3 delta, 4 in, 5 out, 6 fluid list, 7 tag in, 8 tag out, 9 solid list
 void oracle_get_boundary(void *p, int w, int what, void *out) {
     DISPATCH(p, {
         const WallO &W = o->wall[w];
@@ -1139,6 +1195,7 @@ void oracle_get_boundary(void *p, int w, int what, void *out) {
             case 6: std::memcpy(out, W.fluid.data(), W.fluid.size() * 8); break;
             case 7: std::memcpy(out, o->tag_in, 1024); break;
             case 8: std::memcpy(out, o->tag_out, 1024); break;
+            case 9: std::memcpy(out, W.solid.data(), W.solid.size() * 8); break;
             default: break;
         }
     });

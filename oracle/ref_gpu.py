@@ -9,8 +9,9 @@ for the same case and step count.
 
 Steps:
   stage  (here, where the reference tree is)  copy MRLBM_3D into baseline/_ref/<tag>/ and set
-         the run length and output cadence in the copy's cases/cylinder/outputs.cuh (and the
-         diameter in constants.cuh for the larger timing case); nothing else is changed.
+         the run length and output cadence in the copy's cases/cylinder/outputs.cuh (and, in
+         constants.cuh, the diameter for the larger timing case or Z_PERIODIC 0 for the
+         z-wall case); nothing else is changed.
   check  (on the GPU machine)  the reference kernels dereference host-allocated case structs
          (cases/cylinder/cylinder_kernels.cu:7-44 passes `new`-allocated structs to kernels),
          which is only valid where the GPU can access pageable host memory; refuse to run
@@ -58,7 +59,7 @@ def _replace_once(path: Path, old: str, new: str):
     path.write_text("\n".join(lines))
 
 
-def stage(tag: str, steps: int, stats: bool, checkpoint: bool, diameter: int | None):
+def stage(tag: str, steps: int, stats: bool, checkpoint: bool, diameter: int | None, z_walls: bool = False):
     if not REF_TREE.is_dir():
         raise SystemExit("the reference tree is not available here; stage where it is")
     dst = STAGE / tag
@@ -77,7 +78,10 @@ def stage(tag: str, steps: int, stats: bool, checkpoint: bool, diameter: int | N
     if diameter is not None:
         _replace_once(src / "cases" / "cylinder" / "constants.cuh", "constexpr int D = 16;",
                       f"constexpr int D = {diameter};")
-    cfg = {"tag": tag, "steps": steps, "stats": stats, "checkpoint": checkpoint, "diameter": diameter or 16}
+    if z_walls:
+        _replace_once(src / "cases" / "cylinder" / "constants.cuh", "#define Z_PERIODIC 1", "#define Z_PERIODIC 0")
+    cfg = {"tag": tag, "steps": steps, "stats": stats, "checkpoint": checkpoint, "diameter": diameter or 16,
+           "z_walls": z_walls}
     (dst / "config.json").write_text(json.dumps(cfg))
     print(f"staged {dst}")
 
@@ -125,6 +129,7 @@ def main():
     s.add_argument("--no-stats", action="store_true")
     s.add_argument("--no-checkpoint", action="store_true")
     s.add_argument("--diameter", type=int)
+    s.add_argument("--z-walls", action="store_true", help="build with Z_PERIODIC 0 (BCSOLID nodes)")
     sub.add_parser("check")
     b = sub.add_parser("build")
     b.add_argument("tag")
@@ -132,7 +137,7 @@ def main():
     r.add_argument("tag")
     a = ap.parse_args()
     if a.cmd == "stage":
-        stage(a.tag, a.steps, not a.no_stats, not a.no_checkpoint, a.diameter)
+        stage(a.tag, a.steps, not a.no_stats, not a.no_checkpoint, a.diameter, a.z_walls)
     elif a.cmd == "check":
         check()
     elif a.cmd == "build":

@@ -1,6 +1,7 @@
 // Geometry pin: drives the reference's own host-side node classification
-// (sakthi-lbm/MRLBM_3D_CUDA, shipped cylinder case) and dumps its result, so the oracle's
-// and the product's restatements can be checked against it.  Test infrastructure only.
+// (sakthi-lbm/MRLBM_3D_CUDA, shipped cylinder case, and the same case with Z_PERIODIC 0 for
+// the BCSOLID nodes of cases/cylinder/nodeClass.cuh:254-287) and dumps its result, so the
+// oracle's and the product's restatements can be checked against it.  Test infrastructure only.
 //
 // Compiled by oracle/build_ref.py from the reference sources where they lie
 // (-I <reference>/MRLBM_3D/src); nothing here runs on a GPU: only inline host functions of
@@ -44,13 +45,18 @@ int main(int argc, char **argv) {
     b.unit_ny = (real *)malloc(b.NB * sizeof(real));
     b.delta_w = (real *)malloc(b.NB * sizeof(real));
     b.bcfluidList = (size_t *)malloc((b.NB_FLUID > 0 ? b.NB_FLUID : 1) * sizeof(size_t));
+#if Z_PERIODIC
+    b.NB_SOLID = 0;  // only classified without z periodicity
+#endif
+    b.bcsolidList = (size_t *)malloc((b.NB_SOLID > 0 ? b.NB_SOLID : 1) * sizeof(size_t));
     buildBoundaryList_updateBoundaryNodeType(h, b, NODE_INNER, NODE_BCFLUID_INNER, NODE_BCSOLID_INNER);
     assignBoundaryIndices(h, b, NODE_INNER);
     compute_unit_vectors_boundary_nodes(h, b, D_WALL);
     find_incomings_outgoings(h, b);
     setup_bcfluid_masks(h, b);
+    setup_bcsolid_masks(h, b);
 
-    const int meta[8] = {NX, NY, NZ, b.NB, b.NB_FLUID, 0, 0, 0};
+    const int meta[8] = {NX, NY, NZ, b.NB, b.NB_FLUID, b.NB_SOLID, Z_PERIODIC, 0};
     const float fmeta[4] = {XC, YC, D_WALL, (float)OMEGA};
     dump(out, "meta.i32", meta, sizeof(meta));
     dump(out, "meta.f32", fmeta, sizeof(fmeta));
@@ -64,6 +70,7 @@ int main(int argc, char **argv) {
     dump(out, "bcfluid_list_tiled.u64", b.bcfluidList, b.NB_FLUID * sizeof(size_t));
     dump(out, "tag_in_mask.u32", h_incomingMask_bcfluid, sizeof(h_incomingMask_bcfluid));
     dump(out, "tag_out_mask.u32", h_outgoingMask_bcfluid, sizeof(h_outgoingMask_bcfluid));
-    printf("NB=%d NB_FLUID=%d\n", b.NB, b.NB_FLUID);
+    dump(out, "bcsolid_list_tiled.u64", b.bcsolidList, b.NB_SOLID * sizeof(size_t));
+    printf("NB=%d NB_FLUID=%d NB_SOLID=%d\n", b.NB, b.NB_FLUID, b.NB_SOLID);
     return 0;
 }

@@ -7,6 +7,10 @@ sources by oracle/build_ref.py).  Index arrays are converted from the reference'
 IDX_BLOCK order to lexicographic x + NX (y + NY z); the full node-type array is stored
 lexicographic too.
 
+ref_cylinder_zwall_geometry.npz — the same for that case with z walls (Z_PERIODIC 0,
+oracle/_ref/ref_geometry_zwall): adds the BCSOLID nodes on the z = 0 and z = NZ - 1 faces
+(cases/cylinder/nodeClass.cuh:254-287) and their list.
+
 Run from the repository root where the reference tree is mounted:
     python tests/golden/make_golden.py
 """
@@ -22,7 +26,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
-from oracle.build_ref import build_ref_geometry  # noqa: E402
+from oracle.build_ref import build_ref_geometry, build_ref_geometry_zwall  # noqa: E402
 
 
 def tiled_to_lex(idx: np.ndarray, nx: int, ny: int, nz: int) -> np.ndarray:
@@ -36,8 +40,8 @@ def tiled_to_lex(idx: np.ndarray, nx: int, ny: int, nz: int) -> np.ndarray:
     return x + nx * (y + ny * z)
 
 
-def make_geometry(out: Path):
-    exe = build_ref_geometry()
+def make_geometry(out: Path, zwall: bool = False):
+    exe = build_ref_geometry_zwall() if zwall else build_ref_geometry()
     if exe is None:
         raise SystemExit("reference tree not present: cannot regenerate")
     with tempfile.TemporaryDirectory() as td:
@@ -46,7 +50,7 @@ def make_geometry(out: Path):
         rd = lambda name, dt: np.fromfile(d / name, dtype=dt)  # noqa: E731
         meta = rd("meta.i32", np.int32)
         fmeta = rd("meta.f32", np.float32)
-        nx, ny, nz, nb, nbf = (int(v) for v in meta[:5])
+        nx, ny, nz, nb, nbf, nbs = (int(v) for v in meta[:6])
         types_tiled = rd("node_type_tiled.u32", np.uint32)
         lex = tiled_to_lex(np.arange(nx * ny * nz), nx, ny, nz)
         types = np.empty_like(types_tiled)
@@ -54,7 +58,7 @@ def make_geometry(out: Path):
         np.savez_compressed(
             out,
             shape=np.array([nx, ny, nz], dtype=np.int32),
-            nb=np.int32(nb), nb_fluid=np.int32(nbf),
+            nb=np.int32(nb), nb_fluid=np.int32(nbf), nb_solid=np.int32(nbs), z_periodic=np.int32(meta[6]),
             xc=fmeta[0], yc=fmeta[1], d_wall=fmeta[2], omega=fmeta[3],
             node_types=types,
             boundary_list=tiled_to_lex(rd("boundary_list_tiled.u64", np.uint64), nx, ny, nz),
@@ -63,10 +67,12 @@ def make_geometry(out: Path):
             in_mask=rd("in_mask.u32", np.uint32), out_mask=rd("out_mask.u32", np.uint32),
             fluid_list=tiled_to_lex(rd("bcfluid_list_tiled.u64", np.uint64), nx, ny, nz),
             tag_in_mask=rd("tag_in_mask.u32", np.uint32), tag_out_mask=rd("tag_out_mask.u32", np.uint32),
+            solid_list=tiled_to_lex(rd("bcsolid_list_tiled.u64", np.uint64), nx, ny, nz),
         )
 
 
 if __name__ == "__main__":
     here = Path(__file__).resolve().parent
-    make_geometry(here / "ref_cylinder_geometry.npz")
-    print("wrote", here / "ref_cylinder_geometry.npz")
+    for name, zwall in (("ref_cylinder_geometry.npz", False), ("ref_cylinder_zwall_geometry.npz", True)):
+        make_geometry(here / name, zwall)
+        print("wrote", here / name)

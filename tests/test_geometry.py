@@ -60,7 +60,44 @@ def test_reference_tiled_layout_round_trip(built, golden):
     assert np.array_equal(back, golden["node_types"])
 
 
-@pytest.mark.parametrize("name", ["c1", "annulus_small", "annulus_ref", "channel_staircase", "cylinder_box_walls"])
+@pytest.fixture(scope="module")
+def golden_zwall():
+    return np.load(GOLDEN / "ref_cylinder_zwall_geometry.npz")
+
+
+def test_zwall_golden_fixture_is_consistent(golden_zwall):
+    """Z_PERIODIC 0 build of the shipped case: BCSOLID nodes (class 6) only on the z = 0 and
+    z = NZ-1 planes, inside the classification window, with fewer than four bulk octants."""
+    g = golden_zwall
+    t = g["node_types"]
+    cls = t >> 20
+    nx, ny, nz = (int(v) for v in g["shape"])
+    assert int(g["z_periodic"]) == 0
+    assert int(g["nb_solid"]) == int((cls == 6).sum()) == len(g["solid_list"]) > 0
+    z = g["solid_list"] // (nx * ny)
+    assert set(np.unique(z)) == {0, nz - 1}
+    tags = t[g["solid_list"]] & 0xFF
+    assert all(bin(int(v)).count("1") < 4 for v in tags)
+    assert all(int(v) < 16 for v in tags[z == nz - 1]) and all(int(v) % 16 == 0 for v in tags[z == 0])
+    # the eight tags with a closure (boundaries.cuh:1039-1214) all occur
+    assert {7, 11, 13, 14, 112, 176, 208, 224} <= set(int(v) for v in tags)
+
+
+def test_product_and_oracle_zwall_geometry_match_reference(built, golden_zwall):
+    import oracle
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    desc = cases.reference_cylinder(periodic_z=False)
+    s = Simulation(desc, host_only=True)
+    o = oracle.Oracle(desc, 64)
+    assert np.array_equal(s.node_types(), golden_zwall["node_types"])
+    assert np.array_equal(o.node_types(), golden_zwall["node_types"])
+    for b in (s.boundary(0), o.boundary(0)):
+        for k, gk in KEYS + [("solid_list", "solid_list")]:
+            assert np.array_equal(b[k], golden_zwall[gk]), k
+
+
+@pytest.mark.parametrize("name", ["c1", "annulus_small", "annulus_ref", "channel_staircase", "cylinder_box_walls",
+                                  "cylinder_z_walls", "annulus_z_walls"])
 def test_product_and_oracle_classify_alike(built, name):
     import oracle
     from mrlbm_3d_cuda_gb300 import Simulation, cases
@@ -70,14 +107,18 @@ def test_product_and_oracle_classify_alike(built, name):
         "annulus_ref": lambda: cases.reference_annulus(),
         "channel_staircase": lambda: cases.cylinder_channel(64, 32, 8, 8, 20.0, 15.5, 0.05, 40.0, triangular=False),
         "cylinder_box_walls": lambda: cases.cylinder_channel(64, 40, 12, 10, 24.3, 19.7, 0.05, 60.0),
+        "cylinder_z_walls": lambda: cases.cylinder_channel(64, 40, 12, 10, 24.3, 19.7, 0.05, 60.0, periodic_z=False),
+        "annulus_z_walls": lambda: cases.annulus(48, 48, 8, 8.0, 20.0, 0.05, 50.0, periodic_z=False),
     }[name]()
     s = Simulation(desc, host_only=True)
     o = oracle.Oracle(desc, 64)
     assert np.array_equal(s.node_types(), o.node_types())
     for w in range(2 if desc.geometry == 2 else 1):
         bs, bo = s.boundary(w), o.boundary(w)
-        for k, _ in KEYS:
+        for k, _ in KEYS + [("solid_list", "")]:
             assert np.array_equal(bs[k], bo[k]), (w, k)
+    if not desc.periodic[2]:
+        assert (s.node_types() >> 20 == 6).sum() > 0
     cls = s.node_types() >> 20
     assert (cls == 2).any()
     if desc.geometry == 2:

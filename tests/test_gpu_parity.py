@@ -162,6 +162,36 @@ def test_annulus_two_walls(cuda_device):
         assert_forces(res, w, comps=(4,))
 
 
+BCSOLID_TAGS = [7, 11, 13, 14, 112, 176, 208, 224]
+
+
+@pytest.mark.parametrize("geom", ["cylinder", "annulus"])
+def test_z_walls_bcsolid(cuda_device, geom):
+    """No-slip z faces (Z_PERIODIC 0): BACK / FRONT faces and their edges, the BCFLUID nodes
+    above / below the body's end faces and the BCSOLID nodes where the z faces meet the body
+    (boundaries.cuh:1039-1214).  BCSOLID nodes with a closure tag are held at rest: after the
+    collision u = 0 and the diagonal and xy moments stay 0."""
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    if geom == "cylinder":
+        desc = cases.cylinder_channel(64, 40, 12, 10, 24.3, 19.7, 0.05, 60.0, periodic_z=False)
+    else:
+        desc = cases.annulus(48, 48, 8, 8.0, 20.0, 0.05, 50.0, periodic_z=False)
+    res = run_pair(desc, 6, N.INIT_NOISY_UNIFORM, (0.03, 0.01, 0.0, 0.3, 5), fp64=False)
+    assert_fields(res, 0.05, strict=True)
+    t = res["types"]
+    cls, tag = t >> 20, t & 0xFF
+    sel = np.isin(cls, (N.NODE_BCSOLID_INNER, N.NODE_BCSOLID_OUTER)) & np.isin(tag, BCSOLID_TAGS)
+    m = res["gpu"].reshape(10, -1)
+    assert sel.sum() >= 8
+    assert (m[1:8][:, sel] == 0).all()
+    assert np.abs(m[8:10][:, sel]).max() > 0
+    res = run_pair(desc, 60, N.INIT_REST, forces=True)
+    assert_fields(res, 0.05)
+    if geom == "cylinder":
+        assert_forces(res, 0, comps=(0, 1))
+
+
 def test_staircase_classification(cuda_device):
     from mrlbm_3d_cuda_gb300 import cases
     from mrlbm_3d_cuda_gb300 import native as N

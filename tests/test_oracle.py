@@ -134,3 +134,63 @@ def test_channel_walls_hold_no_slip(built):
     assert np.abs(m[1][walls]).max() == 0.0 and np.abs(m[2][walls]).max() == 0.0
     inlet = t == 11
     assert np.allclose(m[1][inlet], 0.05)
+
+
+def test_z_wall_bcsolid_nodes_rest_and_balance(built):
+    """Z walls (Z_PERIODIC 0): the BCSOLID nodes with a closure tag leave each step at rest
+    (u = 0, mxx = myy = mzz = mxy = 0), and a fluid at rest is a fixed point of the closure:
+    with every known population at w_q rho0, rhoI = 175/216 rho0 and
+    rhoI mxzI = rhoI myzI = 1/216 rho0 give rho (874 + omega) = 108 (10 rhoI + 2 (omega - 1)
+    / 216) = (874 + omega) rho0 and mxz = myz = 0 (boundaries.cuh:1039-1214)."""
+    import oracle
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    desc = cases.cylinder_channel(64, 40, 12, 10, 24.3, 19.7, 0.05, 60.0, periodic_z=False)
+    o = oracle.Oracle(desc, 64)
+    o.init(N.INIT_NOISY_UNIFORM, (0.03, 0.01, 0.0, 0.3, 5))
+    o.step(3)
+    m = o.moments().reshape(10, -1)
+    t = o.node_types()
+    sel = np.isin(t >> 20, (N.NODE_BCSOLID_INNER, N.NODE_BCSOLID_OUTER)) & \
+        np.isin(t & 0xFF, (7, 11, 13, 14, 112, 176, 208, 224))
+    assert sel.sum() >= 8
+    assert (m[1:8][:, sel] == 0.0).all()
+    assert np.abs(m[8:10][:, sel]).max() > 1e-4
+    o.close()
+    rest = oracle.Oracle(desc, 64)
+    rest.init(N.INIT_REST)
+    rest.step(1)  # neighbours are still exactly at rest after one step
+    mr = rest.moments().reshape(10, -1)
+    assert np.abs(mr[:, sel]).max() < 1e-14
+    rest.close()
+
+
+@pytest.mark.parametrize("fixture", ["ref_cylinder_run_n10.npz", "ref_cylinder_run_n160.npz",
+                                     "ref_cylinder_zwall_run_n160.npz"])
+def test_fp32_oracle_matches_reference_build(built, fixture):
+    """The oracle pinned against the reference's own GPU build (fixtures made from its
+    restart.bin and forces.dat, see tests/golden/make_ref_run_golden.py): the shipped cylinder
+    case from the reference's initial state, 11 and 161 steps, and 161 steps of that case
+    built with z walls (Z_PERIODIC 0, BCSOLID nodes).  FP32 oracle fields within
+    1e-5 (per-field scale: rho 1, u U, m cs2) at the sampled nodes; once the drag has
+    developed, Fx and Fy of the last step within 1e-5 of |Fx|."""
+    import oracle
+    from conftest import GOLDEN, field_errors
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    from tests.golden.make_golden import tiled_to_lex
+    g = np.load(GOLDEN / fixture)
+    steps = int(g["steps"])
+    o = oracle.Oracle(cases.reference_cylinder(periodic_z=not int(g.get("z_walls", 0))), 32)
+    o.init(N.INIT_REFERENCE_NOISE)
+    o.step(steps - 1)
+    o.step(1, forces=True)
+    m = o.moments().reshape(10, -1)[:, tiled_to_lex(g["idx"], *g["nxyz"])]
+    err = field_errors(m, g["moments"], 0.1)[:, 0]
+    assert err.max() <= 1e-5, np.array2string(err, precision=3)
+    ref = g["forces"][-1]
+    assert int(ref[0]) == steps - 1
+    if abs(ref[1]) > 1.0:
+        f = o.forces()[0]
+        assert abs(f[0] - ref[1]) <= 1e-5 * abs(ref[1]) and abs(f[1] - ref[2]) <= 1e-5 * abs(ref[1])
+    o.close()

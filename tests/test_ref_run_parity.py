@@ -5,6 +5,8 @@ from runs of the reference build staged by oracle/ref_gpu.py) hold the reference
 after N + 1 steps of its shipped cylinder case (336 x 144 x 48, D = 16, Re = 100, U = 0.1,
 periodic y and z, convective outlet) from its own initial state: all 10 moments at every
 non-bulk node plus 40,000 random nodes, whole-grid field statistics, and its forces.dat.
+ref_cylinder_zwall_run_n160.npz is the same case built with Z_PERIODIC 0: no-slip z faces
+and the BCSOLID nodes where they meet the cylinder (boundaries.cuh:1039-1214).
 
 Criteria (per field, metric of conftest.field_errors; s_f = 1 for rho, U for u, cs2 for m):
   * 11 steps: <= 1e-5 against the reference build;
@@ -38,10 +40,10 @@ def tiled_to_lex(idx: np.ndarray, nx: int, ny: int, nz: int) -> np.ndarray:
     return x + nx * (y + ny * z)
 
 
-def run_ours(steps: int):
+def run_ours(steps: int, periodic_z: bool = True):
     from mrlbm_3d_cuda_gb300 import Simulation, cases
     from mrlbm_3d_cuda_gb300 import native as N
-    sim = Simulation(cases.reference_cylinder(), init=False)
+    sim = Simulation(cases.reference_cylinder(periodic_z=periodic_z), init=False)
     sim.init(N.INIT_REFERENCE_NOISE)
     sim.set_sampling(1, 0)
     sim.step(steps)
@@ -74,17 +76,19 @@ def test_eleven_steps_match_reference_build(cuda_device):
     check_common(g, m, st, f)
 
 
-def test_161_steps_match_reference_build(cuda_device):
+@pytest.mark.parametrize("fixture", ["ref_cylinder_run_n160.npz", "ref_cylinder_zwall_run_n160.npz"])
+def test_161_steps_match_reference_build(cuda_device, fixture):
     import oracle
     from mrlbm_3d_cuda_gb300 import cases
     from mrlbm_3d_cuda_gb300 import native as N
-    g = np.load(GOLDEN / "ref_cylinder_run_n160.npz")
+    g = np.load(GOLDEN / fixture)
     steps = int(g["steps"])
-    m, st, f = run_ours(steps)
+    periodic_z = not int(g.get("z_walls", 0))
+    m, st, f = run_ours(steps, periodic_z)
     idx = g["idx"]
     orc = {}
     for bits in (32, 64):
-        o = oracle.Oracle(cases.reference_cylinder(), bits)
+        o = oracle.Oracle(cases.reference_cylinder(periodic_z=periodic_z), bits)
         o.init(N.INIT_REFERENCE_NOISE)
         o.step(steps)
         orc[bits] = o.moments().reshape(10, -1)[:, tiled_to_lex(idx, *g["nxyz"])]
