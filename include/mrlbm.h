@@ -210,12 +210,24 @@ int mrlbm_write_master_pvd(const char *path, int32_t macr_save, int32_t max_iter
  * files from every sample still in the device ring, append = 1 adds the samples taken since
  * the previous call. */
 int mrlbm_write_forces(mrlbm_handle *h, int32_t wall, const char *forces_path, const char *mass_path, int32_t append);
-/* Time-averaged wall pressure over the steps start..end (inclusive; start < 0 switches it off),
- * sampled after each step like compute_surface_pressure (cases/cylinder/cylinder_kernels.cu:
- * 238-283); set before stepping, it restarts the average. */
+/* Statistics window: steps start..end (inclusive; start < 0 switches it off).  After each step
+ * in it, like cylinder_post_process (cases/cylinder/cylinder_kernels.cu:147-175), the
+ * time-averaged wall pressure (compute_surface_pressure, :238-283) and the inlet density
+ * (compute_inlet_average_density, :285-338) are sampled; set before stepping, it restarts both
+ * averages. */
 int mrlbm_set_pressure_window(mrlbm_handle *h, int64_t start, int64_t end);
 /* pressure.dat `theta z Cp` rows per wall node (cases/cylinder/cylinder_kernels.cuh:251-285). */
 int mrlbm_write_pressure(mrlbm_handle *h, int32_t wall, const char *path);
+/* inlet_density.dat `iter rho_in rho_in_average`, %.16f (statistics/stat_header.cuh:53-72):
+ * mean density of the x = 0 face per window step and the running mean of the samples before
+ * it (the reference writes the line before it updates the mean).  append as for
+ * mrlbm_write_forces. */
+int mrlbm_write_inlet_density(mrlbm_handle *h, const char *path, int32_t append);
+/* The grid_layout/*.dat node lists of the z = 0 slice, `x y z type index` per line, into the
+ * directory `dir` (write_geometry_files, cases/cylinder/cylinder_helpers.cuh:388-470):
+ * inner, outer, bcfluid_inner, bcfluid_outer, bcsolid_inner, bcsolid_outer, solid, fluid,
+ * others.  Host only; works on host-only handles. */
+int mrlbm_write_geometry(const mrlbm_handle *h, const char *dir);
 
 /* ---- allocation-free step (no counterpart in the reference) ------------------------------------
  * One time step of a fully periodic box (no walls, no inlet / outlet) from m_in to m_out,

@@ -79,6 +79,7 @@ void free_all(mrlbm_handle *h) {
     f(h->d_stage);
     f(h->d_ps_avg[0]);
     f(h->d_ps_avg[1]);
+    f(h->d_inlet);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     if (h->side_stream) cudaStreamDestroy(h->side_stream);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -306,6 +307,10 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
             // statistics window: the post-step state (buffer parity ^ 1), as the reference's
             // post_process_step samples it
             ++h->ps_count;
+            const int64_t slot = (h->ps_count - 1) % kRing;
+            h->inlet_steps[(size_t)slot] = it;
+            CK(h, launch_inlet_density(h->d_args, h->parity ^ 1, h->storage, h->d_inlet, (int)slot, h->ps_count,
+                                       h->stream));
             for (int w = 0; w < h->geo.n_walls; ++w)
                 CK(h, launch_surface_pressure(h->d_args, h->parity ^ 1, h->storage, w,
                                               (int)h->geo.wall[w].list.size(), h->d_ps_avg[w], h->ps_count,
@@ -338,6 +343,7 @@ struct SavedState {
     void *buf = nullptr;
     int parity = 0, force_every = 0, diag_every = 0;
     int64_t step = 0, force_count = 0, diag_count = 0;
+    int64_t ps_start = -1, ps_end = -1;
 };
 
 int save_state(mrlbm_handle *h, SavedState &st) {
@@ -350,7 +356,10 @@ int save_state(mrlbm_handle *h, SavedState &st) {
     st.step = h->step;
     st.force_count = h->force_count;
     st.diag_count = h->diag_count;
+    st.ps_start = h->ps_start;
+    st.ps_end = h->ps_end;
     h->force_every = h->diag_every = 0;
+    h->ps_start = h->ps_end = -1;  // no statistics-window samples from trial steps
     return MRLBM_OK;
 }
 
@@ -366,6 +375,8 @@ int restore_state(mrlbm_handle *h, SavedState &st) {
     h->step = st.step;
     h->force_count = st.force_count;
     h->diag_count = st.diag_count;
+    h->ps_start = st.ps_start;
+    h->ps_end = st.ps_end;
     return MRLBM_OK;
 }
 

@@ -75,6 +75,11 @@ struct mrlbm_handle {
     int64_t ps_start = -1, ps_end = -1;
     int ps_count = 0;
     double *d_ps_avg[2] = {nullptr, nullptr};
+    // inlet density of the statistics window: [0] running mean, then per sample (rho_in, mean
+    // over the earlier samples); inlet_steps holds the step of each ring slot
+    double *d_inlet = nullptr;
+    std::vector<int64_t> inlet_steps;
+    int64_t inlet_written = 0;
     int64_t force_count = 0, diag_count = 0;
     // staging
     float *d_stage = nullptr;

@@ -138,6 +138,9 @@ int64_t halo_face_floats(int nx, int ny, int nz, int axis);
 cudaError_t launch_halo_export(const StepArgs *ga, int parity, int storage, int64_t n, float *const faces[6],
                                cudaStream_t s);
 // Accumulate the wall pressure of the state in buffer `buf` into a running mean over n_avg samples.
+// Inlet (x = 0 face) mean density into slot `slot` of the statistics ring, running mean in state[0].
+cudaError_t launch_inlet_density(const StepArgs *ga, int buf, int storage, double *state, int slot, int n_avg,
+                                 cudaStream_t s);
 cudaError_t launch_surface_pressure(const StepArgs *ga, int buf, int storage, int wall, int nb, double *avg, int n_avg,
                                     cudaStream_t s);
 

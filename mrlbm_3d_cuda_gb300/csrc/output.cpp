@@ -7,6 +7,8 @@
 //                                        MRLBM_3D/src/output/saveData.cu:3-231
 //   write_forces / write_mass_flux       MRLBM_3D/src/statistics/stat_header.cuh:16-51
 //   write_pressure                       MRLBM_3D/src/cases/cylinder/cylinder_kernels.cuh:251-285
+//   write_average_inlet_density          MRLBM_3D/src/statistics/stat_header.cuh:53-72
+//   write_geometry_files                 MRLBM_3D/src/cases/cylinder/cylinder_helpers.cuh:388-470
 // The byte layouts are kept exactly (they are read by the reference's restart path, ParaView
 // and post/post.py); values come from this solver's FP64 force sums and FP32 (or decoded
 // FP16 / BF16) moments.
@@ -240,9 +242,73 @@ int mrlbm_set_pressure_window(mrlbm_handle *h, int64_t start, int64_t end) {
         if (!h->d_ps_avg[w] && nb > 0) CK(h, cudaMalloc((void **)&h->d_ps_avg[w], nb * sizeof(double)));
         if (nb > 0) CK(h, cudaMemset(h->d_ps_avg[w], 0, nb * sizeof(double)));
     }
+    if (!h->d_inlet) CK(h, cudaMalloc((void **)&h->d_inlet, (1 + 2 * kRing) * sizeof(double)));
+    CK(h, cudaMemset(h->d_inlet, 0, sizeof(double)));
+    h->inlet_steps.assign(kRing, -1);
+    h->inlet_written = 0;
     h->ps_start = start < 0 ? -1 : start;
     h->ps_end = start < 0 ? -1 : end;
     h->ps_count = 0;
+    return MRLBM_OK;
+}
+
+int mrlbm_write_inlet_density(mrlbm_handle *h, const char *path, int32_t append) {
+    if (!h) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null handle");
+    if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
+    if (!path || !h->d_inlet) return fail(h, MRLBM_ERR_INVALID_ARG, "no inlet samples (mrlbm_set_pressure_window)");
+    CK(h, cudaStreamSynchronize(h->stream));
+    const int64_t first = std::max<int64_t>(append ? h->inlet_written : 0, h->ps_count - kRing);
+    const int64_t n = h->ps_count - first;
+    std::vector<double> e((size_t)std::max<int64_t>(n, 0) * 2);
+    for (int64_t c = first; c < h->ps_count; ++c)
+        CK(h, cudaMemcpy(&e[(size_t)(c - first) * 2], h->d_inlet + 1 + (c % kRing) * 2, 2 * sizeof(double),
+                         cudaMemcpyDeviceToHost));
+    std::ofstream out(path, append ? std::ios::app : std::ios::trunc);
+    if (!out) return fail(h, MRLBM_ERR_IO, std::string("cannot open ") + path);
+    out << std::setprecision(16) << std::fixed;
+    for (int64_t k = 0; k < n; ++k)
+        out << h->inlet_steps[(size_t)((first + k) % kRing)] << " " << e[(size_t)k * 2] << " " << e[(size_t)k * 2 + 1]
+            << std::endl;
+    if (!out) return fail(h, MRLBM_ERR_IO, std::string("write failed: ") + path);
+    h->inlet_written = h->ps_count;
+    return MRLBM_OK;
+}
+
+int mrlbm_write_geometry(const mrlbm_handle *h, const char *dir) {
+    if (!h || !dir) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null argument");
+    static const char *names[9] = {"inner.dat",         "outer.dat",         "bcfluid_inner.dat",
+                                   "bcfluid_outer.dat", "bcsolid_inner.dat", "bcsolid_outer.dat",
+                                   "solid.dat",         "fluid.dat",         "others.dat"};
+    std::ofstream f[9];
+    for (int k = 0; k < 9; ++k) {
+        const std::string p = std::string(dir) + "/" + names[k];
+        f[k].open(p, std::ios::trunc);
+        if (!f[k]) return fail(nullptr, MRLBM_ERR_IO, "cannot open " + p);
+    }
+    const Geometry &g = h->geo;
+    const int z = 0;  // the reference writes the z = 0 slice only (Z_SLICE)
+    for (int y = 0; y < g.ny; ++y)
+        for (int x = 0; x < g.nx; ++x) {
+            const int64_t i = x + (int64_t)g.nx * (y + (int64_t)g.ny * z);
+            const uint32_t c = g.cls[i], idx = g.payload[i];
+            int k;
+            switch (c) {
+                case C_INNER: k = 0; break;
+                case C_OUTER: k = 1; break;
+                case C_BCFLUID_INNER: k = 2; break;
+                case C_BCFLUID_OUTER: k = 3; break;
+                case C_BCSOLID_INNER: k = 4; break;
+                case C_BCSOLID_OUTER: k = 5; break;
+                default: {
+                    // the reference tests (type << index) against NODE_SOLID, then NODE_BULK
+                    const uint64_t t = idx < 32 ? (uint64_t)c << idx : ~0ull;
+                    k = t == C_SOLID ? 6 : (t == C_BULK ? 7 : 8);
+                }
+            }
+            f[k] << x << " " << y << " " << z << " " << c << " " << idx << "\n";
+        }
+    for (int k = 0; k < 9; ++k)
+        if (!f[k].flush()) return fail(nullptr, MRLBM_ERR_IO, std::string("write failed: ") + names[k]);
     return MRLBM_OK;
 }
 

@@ -8,6 +8,8 @@
 //   compute_surface_pressure                         MRLBM_3D/src/cases/cylinder/cylinder_kernels.cu:238-283
 //   bilinear_interpolation, surface_pressure_extrapolation
 //                                                    MRLBM_3D/src/boundary/extrapolation_utils.cuh:5-40,109-154
+//   inlet_avg_density / compute_inlet_average_density, the running mean of cylinder_post_process
+//                                                    MRLBM_3D/src/cases/cylinder/cylinder_kernels.cu:147-175,285-338
 // The reference keeps the populations that cross its 8 x 8 x 4 block faces in six arrays
 // between its two kernels; this solver has no such arrays (populations are rebuilt from the
 // post-collision moments inside the fused step), so a checkpoint rebuilds them the same way:
@@ -124,6 +126,39 @@ __global__ void surface_pressure_kernel(const StepArgs *__restrict__ ga, int buf
     avg[i] += (ps - avg[i]) / (double)n_avg;  // running mean over the sampled steps
 }
 
+// Mean density of the x = 0 face (ny * nz nodes) and its running mean over the statistics
+// window.  One block, FP64 sums in a fixed order (the reference sums in FP32 with atomics).
+// state[0] is the running mean; slot entry = (this sample, the mean of the earlier samples):
+// the reference writes its inlet_density.dat line before it updates the mean.
+constexpr int kInletThreads = 512;
+
+template <typename S>
+__global__ void __launch_bounds__(kInletThreads)
+    inlet_density_kernel(const StepArgs *__restrict__ ga, int buf, double *__restrict__ state, int slot, int n_avg) {
+    const StepArgs &a = *ga;
+    const S *m = (const S *)a.m[buf];
+    const int n = a.ny * a.nz;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += kInletThreads) {
+        const int y = i % a.ny, z = i / a.ny;
+        s += (double)(a.rho0 + rho_dev<S>(a, m, 0, y, z));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ double part[kInletThreads / 32];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kInletThreads / 32; ++w) t += part[w];
+        const double in = t / (double)n;
+        double *e = state + 1 + 2 * (int64_t)slot;
+        e[0] = in;
+        e[1] = state[0];
+        state[0] += (in - state[0]) / (double)n_avg;
+    }
+}
+
 }  // namespace
 
 int64_t halo_face_floats(int nx, int ny, int nz, int axis) {
@@ -147,6 +182,21 @@ cudaError_t launch_halo_export(const StepArgs *ga, int parity, int storage, int6
         case MRLBM_STORAGE_BF16:
             halo_export_kernel<__nv_bfloat16><<<blocks, 256, 0, s>>>(ga, parity, faces[0], faces[1], faces[2],
                                                                      faces[3], faces[4], faces[5]);
+            break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_inlet_density(const StepArgs *ga, int buf, int storage, double *state, int slot, int n_avg,
+                                 cudaStream_t s) {
+    switch (storage) {
+        case MRLBM_STORAGE_F32: inlet_density_kernel<float><<<1, kInletThreads, 0, s>>>(ga, buf, state, slot, n_avg); break;
+        case MRLBM_STORAGE_F16:
+            inlet_density_kernel<__half><<<1, kInletThreads, 0, s>>>(ga, buf, state, slot, n_avg);
+            break;
+        case MRLBM_STORAGE_BF16:
+            inlet_density_kernel<__nv_bfloat16><<<1, kInletThreads, 0, s>>>(ga, buf, state, slot, n_avg);
             break;
         default: return cudaErrorInvalidValue;
     }

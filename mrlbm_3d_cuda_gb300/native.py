@@ -105,6 +105,8 @@ _SIGS = {
     "mrlbm_write_forces": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, C.c_int32]),
     "mrlbm_set_pressure_window": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
     "mrlbm_write_pressure": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p]),
+    "mrlbm_write_inlet_density": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32]),
+    "mrlbm_write_geometry": (C.c_int, [C.c_void_p, C.c_char_p]),
     "mrlbm_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "mrlbm_batch_create": (C.c_int, [C.POINTER(CaseDesc), C.c_int32, C.POINTER(C.c_void_p)]),
     "mrlbm_batch_destroy": (C.c_int, [C.c_void_p]),

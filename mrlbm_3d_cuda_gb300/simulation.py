@@ -204,11 +204,20 @@ class Simulation:
         self._ck(N.lib().mrlbm_write_forces(self._h, int(wall), enc(forces_path), enc(mass_path), int(bool(append))))
 
     def set_pressure_window(self, start: int, end: int):
-        """Average the wall pressure over steps start..end (start < 0: off)."""
+        """Statistics window: average the wall pressure and sample the inlet density over
+        steps start..end (start < 0: off)."""
         self._ck(N.lib().mrlbm_set_pressure_window(self._h, int(start), int(end)))
 
     def write_pressure(self, path: str, wall: int = 0):
         self._ck(N.lib().mrlbm_write_pressure(self._h, int(wall), str(path).encode()))
+
+    def write_inlet_density(self, path: str, append: bool = False):
+        """inlet_density.dat (`iter rho_in rho_in_average`) of the statistics window."""
+        self._ck(N.lib().mrlbm_write_inlet_density(self._h, str(path).encode(), int(bool(append))))
+
+    def write_geometry(self, directory: str):
+        """grid_layout/*.dat node lists of the z = 0 slice into `directory`."""
+        self._ck(N.lib().mrlbm_write_geometry(self._h, str(directory).encode()))
 
     def run_reference_outputs(self, out_dir: str, max_iter: int, macr_save: int, stat_start: int, stat_end: int,
                               checkpoint_save: int = 0):
@@ -216,11 +225,15 @@ class Simulation:
         iterations 0..max_iter; data<10000000+it>.vti every macr_save iterations (master.pvd
         lists them); checkpoint/restart.bin (+ restart_step.txt) every checkpoint_save
         iterations after the first; forces / mass flux sampled and the wall pressure averaged
-        over stat_start..stat_end, written as forces.dat, mass_flux.dat and pressure.dat."""
+        over stat_start..stat_end, written as forces.dat, mass_flux.dat, pressure.dat and (cylinder)
+        inlet_density.dat; the node lists of grid_layout/ at the start."""
         import os
         os.makedirs(out_dir, exist_ok=True)
         write_master_pvd(os.path.join(out_dir, "master.pvd"), macr_save, max_iter)
         walls = self.desc.geometry != N.GEOM_NONE
+        if walls:
+            os.makedirs(os.path.join(out_dir, "grid_layout"), exist_ok=True)
+            self.write_geometry(os.path.join(out_dir, "grid_layout"))
         start = int(self.get_info().step)
         if walls:
             self.set_pressure_window(stat_start, stat_end)
@@ -239,6 +252,8 @@ class Simulation:
         if walls:
             self.write_forces(os.path.join(out_dir, "forces.dat"), os.path.join(out_dir, "mass_flux.dat"))
             self.write_pressure(os.path.join(out_dir, "pressure.dat"))
+            if self.desc.geometry == N.GEOM_CYLINDER:
+                self.write_inlet_density(os.path.join(out_dir, "inlet_density.dat"))
 
 
 def write_master_pvd(path: str, macr_save: int, max_iter: int):

@@ -12,7 +12,9 @@
 // cylinder_kernels.cuh:406-465.
 #include <cstdio>
 #include <cstdlib>
+#include <filesystem>
 #include <string>
+#include <unistd.h>
 
 #include "solver/initializeLBM.cuh"
 
@@ -29,9 +31,12 @@ static void dump(const std::string &dir, const char *name, const void *p, size_t
 
 int main(int argc, char **argv) {
     if (argc < 2) {
-        fprintf(stderr, "usage: ref_geometry <out_dir>\n");
+        fprintf(stderr, "usage: ref_geometry <out_dir> [files]\n");
         return 1;
     }
+    // "files": also run the reference's own grid_layout writer (cylinder_helpers.cuh:388-470)
+    // with <out_dir> as the working directory, where it writes OUTPUT/CYLINDER/<ID_SIM>/grid_layout/
+    const bool files = argc > 2 && std::string(argv[2]) == "files";
     const std::string out = argv[1];
     nodeVar h{};
     h.nodeType = (nodeType_t *)calloc(NUM_LBM_NODES, sizeof(nodeType_t));
@@ -71,6 +76,14 @@ int main(int argc, char **argv) {
     dump(out, "tag_in_mask.u32", h_incomingMask_bcfluid, sizeof(h_incomingMask_bcfluid));
     dump(out, "tag_out_mask.u32", h_outgoingMask_bcfluid, sizeof(h_outgoingMask_bcfluid));
     dump(out, "bcsolid_list_tiled.u64", b.bcsolidList, b.NB_SOLID * sizeof(size_t));
+    if (files) {
+        if (chdir(out.c_str()) != 0) {
+            fprintf(stderr, "cannot enter %s\n", out.c_str());
+            return 2;
+        }
+        std::filesystem::create_directories(construct_path(PATH_FILES, ID_SIM, "grid_layout"));
+        write_geometry_files(h);
+    }
     printf("NB=%d NB_FLUID=%d NB_SOLID=%d\n", b.NB, b.NB_FLUID, b.NB_SOLID);
     return 0;
 }

@@ -11,11 +11,16 @@ ref_cylinder_zwall_geometry.npz — the same for that case with z walls (Z_PERIO
 oracle/_ref/ref_geometry_zwall): adds the BCSOLID nodes on the z = 0 and z = NZ - 1 faces
 (cases/cylinder/nodeClass.cuh:254-287) and their list.
 
+ref_geometry_files.json — SHA-256 and size of each grid_layout/*.dat file the reference's own
+write_geometry_files (cases/cylinder/cylinder_helpers.cuh:388-470) writes for both builds.
+
 Run from the repository root where the reference tree is mounted:
     python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
+import hashlib
+import json
 import subprocess
 import sys
 import tempfile
@@ -71,8 +76,24 @@ def make_geometry(out: Path, zwall: bool = False):
         )
 
 
+def make_geometry_files(out: Path):
+    res = {}
+    for variant, build in (("periodic_z", build_ref_geometry), ("z_walls", build_ref_geometry_zwall)):
+        exe = build()
+        if exe is None:
+            raise SystemExit("reference tree not present: cannot regenerate")
+        with tempfile.TemporaryDirectory() as td:
+            subprocess.run([str(exe), td, "files"], check=True, capture_output=True)
+            d = next(Path(td).rglob("grid_layout"))
+            res[variant] = {f.name: {"sha256": hashlib.sha256(f.read_bytes()).hexdigest(), "bytes": f.stat().st_size}
+                            for f in sorted(d.glob("*.dat"))}
+    out.write_text(json.dumps(res, indent=1, sort_keys=True) + "\n")
+
+
 if __name__ == "__main__":
     here = Path(__file__).resolve().parent
     for name, zwall in (("ref_cylinder_geometry.npz", False), ("ref_cylinder_zwall_geometry.npz", True)):
         make_geometry(here / name, zwall)
         print("wrote", here / name)
+    make_geometry_files(here / "ref_geometry_files.json")
+    print("wrote", here / "ref_geometry_files.json")

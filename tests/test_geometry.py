@@ -123,3 +123,20 @@ def test_product_and_oracle_classify_alike(built, name):
     assert (cls == 2).any()
     if desc.geometry == 2:
         assert (cls == 3).any()
+
+
+@pytest.mark.parametrize("variant", ["periodic_z", "z_walls"])
+def test_geometry_files_match_reference_writer(built, tmp_path, variant):
+    """grid_layout/*.dat byte for byte against the reference's own write_geometry_files
+    (cylinder_helpers.cuh:388-470, run by the geometry harness; SHA-256 in the fixture)."""
+    import hashlib
+    import json
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    want = json.loads((GOLDEN / "ref_geometry_files.json").read_text())[variant]
+    s = Simulation(cases.reference_cylinder(periodic_z=variant == "periodic_z"), host_only=True)
+    s.write_geometry(tmp_path)
+    got = {f.name: {"sha256": hashlib.sha256(f.read_bytes()).hexdigest(), "bytes": f.stat().st_size}
+           for f in sorted(tmp_path.glob("*.dat"))}
+    assert got == want
+    if variant == "z_walls":
+        assert want["bcsolid_inner.dat"]["bytes"] > 0

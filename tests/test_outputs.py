@@ -189,6 +189,37 @@ def test_surface_pressure_file(cuda_device, tmp_path):
 
 
 @pytest.mark.gpu
+def test_inlet_density_file(cuda_device, tmp_path):
+    """inlet_density.dat over a statistics window: per step the mean density of the x = 0 face
+    (computed here from the field after each step) and the running mean of the earlier samples
+    (0 on the first line), %.16f."""
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    desc = cases.cylinder_channel(64, 40, 12, 10, 24.3, 19.7, 0.05, 60.0)
+    sim = Simulation(desc, init=False)
+    sim.init(N.INIT_NOISY_UNIFORM, (0.03, 0.01, 0.0, 0.3, 5))
+    sim.set_pressure_window(3, 7)
+    want, mean, n = [], 0.0, 0
+    for it in range(10):
+        sim.step(1)
+        if 3 <= it <= 7:
+            r_in = (np.float32(desc.rho0) + sim.moments()[0][:, :, 0]).astype(np.float64).mean()  # (nz, ny) face
+            want.append((it, r_in, mean))
+            n += 1
+            mean += (r_in - mean) / n
+    p = tmp_path / "inlet_density.dat"
+    sim.write_inlet_density(p)
+    rows = np.loadtxt(p)
+    assert rows.shape == (5, 3)
+    assert list(rows[:, 0].astype(int)) == [w[0] for w in want]
+    assert np.allclose(rows[:, 1], [w[1] for w in want], rtol=0, atol=1e-12)
+    assert np.allclose(rows[:, 2], [w[2] for w in want], rtol=0, atol=1e-12)
+    assert rows[0, 2] == 0.0
+    assert all(len(v.split(".")[1]) == 16 for v in p.read_text().splitlines()[0].split()[1:])
+    sim.close()
+
+
+@pytest.mark.gpu
 def test_reference_style_run_writes_every_output(cuda_device, tmp_path):
     from mrlbm_3d_cuda_gb300 import Simulation, cases
     from mrlbm_3d_cuda_gb300 import native as N
@@ -197,7 +228,9 @@ def test_reference_style_run_writes_every_output(cuda_device, tmp_path):
     sim.run_reference_outputs(tmp_path, max_iter=20, macr_save=10, stat_start=12, stat_end=20, checkpoint_save=10)
     names = sorted(p.name for p in tmp_path.iterdir())
     assert names == ["checkpoint", "data10000000.vti", "data10000010.vti", "data10000020.vti", "forces.dat",
-                     "mass_flux.dat", "master.pvd", "pressure.dat"]
+                     "grid_layout", "inlet_density.dat", "mass_flux.dat", "master.pvd", "pressure.dat"]
+    assert np.loadtxt(tmp_path / "inlet_density.dat").shape == (9, 3)
+    assert len(list((tmp_path / "grid_layout").glob("*.dat"))) == 9
     assert (tmp_path / "checkpoint" / "restart_step.txt").read_text().strip() == "21"
     assert np.loadtxt(tmp_path / "forces.dat").shape == (9, 4)
     sim.close()
