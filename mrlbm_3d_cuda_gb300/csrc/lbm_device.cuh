@@ -27,60 +27,70 @@ struct Mom {
     float mxx, myy, mzz, mxy, mxz, myz;
 };
 
-// f_q = w_q rho [1 + 3 c.u + 4.5 (c_a c_b - delta_ab / 3) m_ab], second-order Hermite.
-// The scaled moments go through __fmul_rn, which is never fused into an FMA: the owner and
-// the rim copies of this function keep different subsets of the populations, and free
-// contraction of `scaled moment + sum` made the two round differently.
+// f_q = w_q rho [1 + 3 c.u + 4.5 (c_a c_b - delta_ab / 3) m_ab], second-order Hermite,
+// as even part +- odd part: w_q rho E_q +- 3 w_q rho (c.u), with E_q built by FMAs from
+// p0 = 1 - 1.5 tr(m).  Every FMA is written out (__fmaf_rn) and every product that must not
+// fuse goes through __fmul_rn: the owner and the rim copies of this function keep different
+// subsets of the populations, and free contraction made the two round differently.
 __device__ __forceinline__ void reconstruct(const Mom &m, float f[27]) {
-    const float ux = __fmul_rn(3.0f, m.ux), uy = __fmul_rn(3.0f, m.uy), uz = __fmul_rn(3.0f, m.uz);
-    const float xx = __fmul_rn(4.5f, m.mxx), yy = __fmul_rn(4.5f, m.myy), zz = __fmul_rn(4.5f, m.mzz);
-    const float xy = __fmul_rn(9.0f, m.mxy), xz = __fmul_rn(9.0f, m.mxz), yz = __fmul_rn(9.0f, m.myz);
-    const float tr = xx + yy + zz;
-    const float p0 = __fmaf_rn(-kCs2, tr, 1.0f);
-    const float r0 = m.rho * kW0, r1 = m.rho * kW1, r2 = m.rho * kW2, r3 = m.rho * kW3;
-    f[0] = r0 * p0;
-    const float ax = p0 + xx, ay = p0 + yy, az = p0 + zz;
-    f[1] = r1 * (ax + ux);
-    f[2] = r1 * (ax - ux);
-    f[3] = r1 * (ay + uy);
-    f[4] = r1 * (ay - uy);
-    f[5] = r1 * (az + uz);
-    f[6] = r1 * (az - uz);
+    const float t = __fadd_rn(__fadd_rn(m.mxx, m.myy), m.mzz);
+    const float p0 = __fmaf_rn(-1.5f, t, 1.0f);
+    const float ax = __fmaf_rn(4.5f, m.mxx, p0), ay = __fmaf_rn(4.5f, m.myy, p0), az = __fmaf_rn(4.5f, m.mzz, p0);
+    const float r1 = __fmul_rn(m.rho, kW1), r2 = __fmul_rn(m.rho, kW2), r3 = __fmul_rn(m.rho, kW3);
+    const float q1 = __fmul_rn(3.0f, r1), q2 = __fmul_rn(3.0f, r2), q3 = __fmul_rn(3.0f, r3);
+    const float n2 = __fmul_rn(9.0f, r2), n3 = __fmul_rn(9.0f, r3);
+    f[0] = __fmul_rn(__fmul_rn(m.rho, kW0), p0);
     {
-        const float b = ax + yy, sp = ux + uy, sm = ux - uy, cp = b + xy, cm = b - xy;
-        f[7] = r2 * (cp + sp);
-        f[8] = r2 * (cp - sp);
-        f[13] = r2 * (cm + sm);
-        f[14] = r2 * (cm - sm);
+        const float ex = __fmul_rn(r1, ax), ey = __fmul_rn(r1, ay), ez = __fmul_rn(r1, az);
+        f[1] = __fmaf_rn(q1, m.ux, ex);
+        f[2] = __fmaf_rn(-q1, m.ux, ex);
+        f[3] = __fmaf_rn(q1, m.uy, ey);
+        f[4] = __fmaf_rn(-q1, m.uy, ey);
+        f[5] = __fmaf_rn(q1, m.uz, ez);
+        f[6] = __fmaf_rn(-q1, m.uz, ez);
+    }
+    const float upp = __fadd_rn(m.ux, m.uy), upm = __fsub_rn(m.ux, m.uy);
+    {
+        const float b = __fmul_rn(r2, __fmaf_rn(4.5f, m.myy, ax));
+        const float cp = __fmaf_rn(n2, m.mxy, b), cm = __fmaf_rn(-n2, m.mxy, b);
+        f[7] = __fmaf_rn(q2, upp, cp);
+        f[8] = __fmaf_rn(-q2, upp, cp);
+        f[13] = __fmaf_rn(q2, upm, cm);
+        f[14] = __fmaf_rn(-q2, upm, cm);
     }
     {
-        const float b = ax + zz, sp = ux + uz, sm = ux - uz, cp = b + xz, cm = b - xz;
-        f[9] = r2 * (cp + sp);
-        f[10] = r2 * (cp - sp);
-        f[15] = r2 * (cm + sm);
-        f[16] = r2 * (cm - sm);
+        const float b = __fmul_rn(r2, __fmaf_rn(4.5f, m.mzz, ax));
+        const float cp = __fmaf_rn(n2, m.mxz, b), cm = __fmaf_rn(-n2, m.mxz, b);
+        const float sp = __fadd_rn(m.ux, m.uz), sm = __fsub_rn(m.ux, m.uz);
+        f[9] = __fmaf_rn(q2, sp, cp);
+        f[10] = __fmaf_rn(-q2, sp, cp);
+        f[15] = __fmaf_rn(q2, sm, cm);
+        f[16] = __fmaf_rn(-q2, sm, cm);
     }
     {
-        const float b = ay + zz, sp = uy + uz, sm = uy - uz, cp = b + yz, cm = b - yz;
-        f[11] = r2 * (cp + sp);
-        f[12] = r2 * (cp - sp);
-        f[17] = r2 * (cm + sm);
-        f[18] = r2 * (cm - sm);
+        const float b = __fmul_rn(r2, __fmaf_rn(4.5f, m.mzz, ay));
+        const float cp = __fmaf_rn(n2, m.myz, b), cm = __fmaf_rn(-n2, m.myz, b);
+        const float sp = __fadd_rn(m.uy, m.uz), sm = __fsub_rn(m.uy, m.uz);
+        f[11] = __fmaf_rn(q2, sp, cp);
+        f[12] = __fmaf_rn(-q2, sp, cp);
+        f[17] = __fmaf_rn(q2, sm, cm);
+        f[18] = __fmaf_rn(-q2, sm, cm);
     }
     {
-        const float c0 = p0 + tr;
-        const float a = xy + xz, b = xy - xz;
-        const float upp = ux + uy, upm = ux - uy;
-        const float s1 = upp + uz, s2 = upp - uz, s3 = upm + uz, s4 = upm - uz;
-        const float e1 = c0 + (a + yz), e2 = c0 + (b - yz), e3 = c0 - (b + yz), e4 = c0 - (a - yz);
-        f[19] = r3 * (e1 + s1);
-        f[20] = r3 * (e1 - s1);
-        f[21] = r3 * (e2 + s2);
-        f[22] = r3 * (e2 - s2);
-        f[23] = r3 * (e3 + s3);
-        f[24] = r3 * (e3 - s3);
-        f[26] = r3 * (e4 + s4);
-        f[25] = r3 * (e4 - s4);
+        const float c0 = __fmul_rn(r3, __fmaf_rn(4.5f, t, p0));
+        const float a = __fadd_rn(m.mxy, m.mxz), b = __fsub_rn(m.mxy, m.mxz);
+        const float e1 = __fmaf_rn(n3, __fadd_rn(a, m.myz), c0), e2 = __fmaf_rn(n3, __fsub_rn(b, m.myz), c0);
+        const float e3 = __fmaf_rn(-n3, __fadd_rn(b, m.myz), c0), e4 = __fmaf_rn(-n3, __fsub_rn(a, m.myz), c0);
+        const float s1 = __fadd_rn(upp, m.uz), s2 = __fsub_rn(upp, m.uz);
+        const float s3 = __fadd_rn(upm, m.uz), s4 = __fsub_rn(upm, m.uz);
+        f[19] = __fmaf_rn(q3, s1, e1);
+        f[20] = __fmaf_rn(-q3, s1, e1);
+        f[21] = __fmaf_rn(q3, s2, e2);
+        f[22] = __fmaf_rn(-q3, s2, e2);
+        f[23] = __fmaf_rn(q3, s3, e3);
+        f[24] = __fmaf_rn(-q3, s3, e3);
+        f[26] = __fmaf_rn(q3, s4, e4);
+        f[25] = __fmaf_rn(-q3, s4, e4);
     }
 }
 
