@@ -8,10 +8,18 @@
 
 namespace mrlbm {
 
-// x-blocked, field-interleaved moment layout (see storage.cuh).
+// x-blocked, field-interleaved moment layout (see storage.cuh): each 32-node run of an
+// (y, z) row owns 10 x 32 consecutive elements.  `esz` is the element size: 4-byte storage
+// keeps one field per 32-node line; 2-byte storage keeps the field pairs (2j, 2j+1) of a node
+// in one 32-bit word, so a lane moves two fields per access.  aos_index is the element of a
+// node's field 0, field_offset the distance of field k from it.
 constexpr int kXBlock = 32;
-inline __host__ __device__ int64_t aos_index(int x, int y, int z, int nxb, int ny) {
-    return ((((int64_t)z * ny + y) * nxb + (x >> 5)) * 10) * kXBlock + (x & (kXBlock - 1));
+inline __host__ __device__ int64_t aos_index(int x, int y, int z, int nxb, int ny, int esz) {
+    const int64_t run = ((((int64_t)z * ny + y) * nxb + (x >> 5)) * 10) * kXBlock;
+    return run + (esz == 4 ? (x & (kXBlock - 1)) : 2 * (x & (kXBlock - 1)));
+}
+inline __host__ __device__ constexpr int field_offset(int k, int esz) {
+    return esz == 4 ? k * kXBlock : (k >> 1) * (2 * kXBlock) + (k & 1);
 }
 inline __host__ __device__ int64_t aos_elements(int nx, int ny, int nz) {
     return (int64_t)nz * ny * ((nx + kXBlock - 1) / kXBlock) * 10 * kXBlock;

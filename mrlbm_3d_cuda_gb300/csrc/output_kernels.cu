@@ -49,7 +49,7 @@ __global__ void halo_export_kernel(const StepArgs *__restrict__ ga, int parity, 
     if (!(wx || ex || sy || ny_ || bz || fz)) return;
     const int64_t gx = a.nx / kBX, gy = a.ny / kBY;
     const int64_t block = x / kBX + gx * (y / kBY + gy * (z / kBZ));
-    const Mom m = load_mom<S>((const S *)a.m[parity], aos_index(x, y, z, a.nxb, a.ny), a.rho0, a.sc);
+    const Mom m = load_mom<S>((const S *)a.m[parity], aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S)), a.rho0, a.sc);
     float f[27];
     reconstruct(m, f);
 #pragma unroll
@@ -69,7 +69,7 @@ __global__ void halo_export_kernel(const StepArgs *__restrict__ ga, int parity, 
 // Density deviation at (x, y, z) of the stored moments.
 template <typename S>
 __device__ __forceinline__ float rho_dev(const StepArgs &a, const S *m, int x, int y, int z) {
-    const float v = to_f<S>(m[aos_index(x, y, z, a.nxb, a.ny)]);
+    const float v = to_f<S>(m[aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S))]);
     return std::is_same<S, float>::value ? v : v * a.sc.is[0];
 }
 

@@ -52,7 +52,7 @@ __device__ __noinline__ Mom pulled_rho_u(const StepArgs &a, const S *__restrict_
 #pragma unroll 1
     for (int q = 0; q < 27; ++q) {
         const int xs = (x - cxq(q) + a.nx) % a.nx, ys = (y - cyq(q) + a.ny) % a.ny, zs = (z - czq(q) + a.nz) % a.nz;
-        const Mom mq = load_mom<S>(src, aos_index(xs, ys, zs, a.nxb, a.ny), a.rho0, a.sc);
+        const Mom mq = load_mom<S>(src, aos_index(xs, ys, zs, a.nxb, a.ny, (int)sizeof(S)), a.rho0, a.sc);
         float g[27];
         reconstruct(mq, g);
         f[q] = g[q];
@@ -73,7 +73,7 @@ __device__ __forceinline__ int special_node(const StepArgs &a, int parity, bool 
     if (cls == C_BULK) {
         evaluate(fl, m);
     } else {
-        const Mom prev = load_mom<S>(src, aos_index(x, y, z, a.nxb, a.ny), a.rho0, a.sc);
+        const Mom prev = load_mom<S>(src, aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S)), a.rho0, a.sc);
         m = prev;  // nodes without a closure keep their pre-stream moments
         if (cls == C_SOLID) {
             fluid = false;
@@ -106,7 +106,7 @@ __device__ __forceinline__ int special_node(const StepArgs &a, int parity, bool 
                     c.west_prev = pulled_rho_u<S>(a, src, x - 1, y, z);
                     c.self_prev = rho_u_of(fl);
                 } else {
-                    c.west_prev = load_mom<S>(src, aos_index(x - 1, y, z, a.nxb, a.ny), a.rho0, a.sc);
+                    c.west_prev = load_mom<S>(src, aos_index(x - 1, y, z, a.nxb, a.ny, (int)sizeof(S)), a.rho0, a.sc);
                 }
             }
             Mom o = prev;
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kListThreads)
         const int slot = a.tile_slot[ty * a.tiles_x + tx];
         Mom m;
         const int code = special_node<S>(a, parity, force != 0, w, f, x, y, z, slot, tx * TILE_X, ty * a.tile_y, m);
-        if (code) store_mom<S>(dst, aos_index(x, y, z, a.nxb, a.ny), m, a.rho0, a.sc);
+        if (code) store_mom<S>(dst, aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S)), m, a.rho0, a.sc);
         if (code == 2 && diag_part) {
             dm += (double)(m.rho - a.rho0);
             de += 0.5 * (double)(m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);

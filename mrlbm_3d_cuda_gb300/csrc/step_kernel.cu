@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         int64_t cxy = 0;
         bool active = own;
         if (own) {
-            cxy = aos_index(x, y, 0, nxb, ny);
+            cxy = aos_index(x, y, 0, nxb, ny, (int)sizeof(S));
         } else if (!owner) {
             int rx, ry, sd;
             const int r = tid - G::NOWN;
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 int gx = x0 + rx, gy = y0 + ry;
                 gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
                 gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
-                cxy = aos_index(gx, gy, 0, nxb, ny);
+                cxy = aos_index(gx, gy, 0, nxb, ny, (int)sizeof(S));
                 active = true;
             }
         }

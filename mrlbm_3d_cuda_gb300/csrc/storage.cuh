@@ -1,8 +1,10 @@
 // Moment storage in HBM, x-blocked and field-interleaved: the 32 nodes x = 32 b .. 32 b + 31 of
 // one (y, z) row keep their 10 fields (rho - rho0, ux, uy, uz, mxx, myy, mzz, mxy, mxz, myz)
-// in one contiguous run of 10 x 32 values, so a warp reads or writes a field of its row as
-// one 128-byte line and all 10 fields of a node sit at constant offsets from one address.
-// FP32, or FP16 / BF16 holding scaled deviations from the rest state (rho0, u = 0, m = 0).
+// in one contiguous run of 10 x 32 values, and all 10 fields of a node sit at constant
+// offsets from one address.  FP32 keeps one field per 128-byte line (a warp moves a field of
+// its row per access); FP16 / BF16 hold scaled deviations from the rest state (rho0, u = 0,
+// m = 0) with the field pairs (2j, 2j+1) of a node in one 32-bit word, so a warp moves two
+// fields of its row per 128-byte access (kernels.h: aos_index, field_offset).
 #pragma once
 
 #include <cuda_bf16.h>
@@ -53,12 +55,55 @@ __device__ __forceinline__ Mom decode(const float v[10], float rho0, const Stora
     return m;
 }
 
-// `ai` is the element index of field 0 of a node (aos_index); field k sits at ai + 32 k.
+// Two 16-bit values of one 32-bit word (lower address first) <-> two floats.
+template <typename S>
+__device__ __forceinline__ float2 pair_to_f(uint32_t w);
+template <>
+__device__ __forceinline__ float2 pair_to_f<__half>(uint32_t w) {
+    __half2 h;
+    memcpy(&h, &w, 4);
+    return __half22float2(h);
+}
+template <>
+__device__ __forceinline__ float2 pair_to_f<__nv_bfloat16>(uint32_t w) {
+    __nv_bfloat162 h;
+    memcpy(&h, &w, 4);
+    return __bfloat1622float2(h);
+}
+template <typename S>
+__device__ __forceinline__ uint32_t pair_from_f(float a, float b);
+template <>
+__device__ __forceinline__ uint32_t pair_from_f<__half>(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    uint32_t w;
+    memcpy(&w, &h, 4);
+    return w;
+}
+template <>
+__device__ __forceinline__ uint32_t pair_from_f<__nv_bfloat16>(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    uint32_t w;
+    memcpy(&w, &h, 4);
+    return w;
+}
+
+// `ai` is the element index of field 0 of a node (aos_index); field k sits at
+// ai + field_offset(k): 32 k for FP32, 64 (k / 2) + k % 2 for FP16 / BF16 (ai is even there).
 template <typename S>
 __device__ __forceinline__ void load_raw(const S *__restrict__ base, int64_t ai, float v[10]) {
-    const S *p = base + ai;
+    if constexpr (std::is_same<S, float>::value) {
+        const float *p = base + ai;
 #pragma unroll
-    for (int k = 0; k < 10; ++k) v[k] = to_f<S>(p[k * kXBlock]);
+        for (int k = 0; k < 10; ++k) v[k] = p[k * kXBlock];
+    } else {
+        const uint32_t *p = reinterpret_cast<const uint32_t *>(base + ai);
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+            const float2 f = pair_to_f<S>(p[j * kXBlock]);
+            v[2 * j] = f.x;
+            v[2 * j + 1] = f.y;
+        }
+    }
 }
 
 template <typename S>
@@ -84,16 +129,12 @@ __device__ __forceinline__ void store_mom(S *__restrict__ base, int64_t ai, cons
         p[8 * kXBlock] = m.mxz;
         p[9 * kXBlock] = m.myz;
     } else {
-        p[0 * kXBlock] = from_f<S>((m.rho - rho0) * sc.s[0]);
-        p[1 * kXBlock] = from_f<S>(m.ux * sc.s[1]);
-        p[2 * kXBlock] = from_f<S>(m.uy * sc.s[1]);
-        p[3 * kXBlock] = from_f<S>(m.uz * sc.s[1]);
-        p[4 * kXBlock] = from_f<S>(m.mxx * sc.s[2]);
-        p[5 * kXBlock] = from_f<S>(m.myy * sc.s[2]);
-        p[6 * kXBlock] = from_f<S>(m.mzz * sc.s[2]);
-        p[7 * kXBlock] = from_f<S>(m.mxy * sc.s[2]);
-        p[8 * kXBlock] = from_f<S>(m.mxz * sc.s[2]);
-        p[9 * kXBlock] = from_f<S>(m.myz * sc.s[2]);
+        uint32_t *w = reinterpret_cast<uint32_t *>(p);
+        w[0 * kXBlock] = pair_from_f<S>((m.rho - rho0) * sc.s[0], m.ux * sc.s[1]);
+        w[1 * kXBlock] = pair_from_f<S>(m.uy * sc.s[1], m.uz * sc.s[1]);
+        w[2 * kXBlock] = pair_from_f<S>(m.mxx * sc.s[2], m.myy * sc.s[2]);
+        w[3 * kXBlock] = pair_from_f<S>(m.mzz * sc.s[2], m.mxy * sc.s[2]);
+        w[4 * kXBlock] = pair_from_f<S>(m.mxz * sc.s[2], m.myz * sc.s[2]);
     }
 }
 

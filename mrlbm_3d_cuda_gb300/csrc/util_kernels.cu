@@ -81,7 +81,7 @@ __global__ void init_kernel(const InitArgs a) {
         }
         default: break;
     }
-    const int64_t ai = aos_index(x, y, z, (a.nx + kXBlock - 1) / kXBlock, a.ny);
+    const int64_t ai = aos_index(x, y, z, (a.nx + kXBlock - 1) / kXBlock, a.ny, (int)sizeof(S));
     store_mom<S>((S *)a.m_a, ai, m, a.rho0, a.sc);
     store_mom<S>((S *)a.m_b, ai, m, a.rho0, a.sc);
 }
@@ -94,20 +94,20 @@ __global__ void convert_kernel(const S *src, S *dst_a, S *dst_b, float *f32, uin
     if (i >= n) return;
     const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((int64_t)nx * ny));
     const int64_t h = layout == MRLBM_LAYOUT_REF_TILED ? ref_tiled_index(x, y, z, nx, ny) : i;
-    const int64_t ai = aos_index(x, y, z, (nx + kXBlock - 1) / kXBlock, ny);
+    const int64_t ai = aos_index(x, y, z, (nx + kXBlock - 1) / kXBlock, ny, (int)sizeof(S));
     int slot = 0;
     for (int f = 0; f < 10; ++f) {
         if (!(mask & (1u << f))) continue;
         const float s = sc.s[scale_class(f)], is = sc.is[scale_class(f)];
         const bool lowp = !std::is_same<S, float>::value;
         if (dir == 0) {
-            const float v = to_f<S>(src[ai + f * kXBlock]);
+            const float v = to_f<S>(src[ai + field_offset(f, (int)sizeof(S))]);
             f32[(int64_t)slot * n + h] = lowp ? v * is : v;
         } else {
             const float v = f32[(int64_t)slot * n + h];
             const S sv = from_f<S>(lowp ? v * s : v);
-            dst_a[ai + f * kXBlock] = sv;
-            if (dst_b) dst_b[ai + f * kXBlock] = sv;
+            dst_a[ai + field_offset(f, (int)sizeof(S))] = sv;
+            if (dst_b) dst_b[ai + field_offset(f, (int)sizeof(S))] = sv;
         }
         ++slot;
     }
