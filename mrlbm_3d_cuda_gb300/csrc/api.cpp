@@ -276,6 +276,7 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
         L.ga = h->d_args;
         L.parity = h->parity;
         L.n_ctas = h->n_ctas;
+        L.full_tiles = h->d.nx % TILE_X == 0 && h->d.ny % h->tile_y == 0;
         if (fs) {
             const int64_t slot = h->force_count % kRing;
             L.force = h->d_force_ring + slot * 10;

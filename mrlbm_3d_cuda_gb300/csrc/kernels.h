@@ -94,6 +94,7 @@ struct StepLaunch {
     double *force = nullptr;       // [2][5] FP64 accumulators of a sampled step, or null
     double *diag_part = nullptr;   // [grid][2] per-CTA mass / energy partials, or null
     int n_ctas = 0;
+    bool full_tiles = false;       // every tile whole (nx % 32 == 0, ny % tile_y == 0)
 };
 
 // Stencil-buffer index of node (x, y, z) for a special tile slot.

@@ -200,6 +200,8 @@ __device__ __forceinline__ void nb_arrive(int id, int n) {
 }
 
 // SPECIAL = false: every node of every item is a plain bulk node (no node words are read).
+// FULL = true: every tile is a whole 32 x TY tile (nx % 32 == 0, ny % TY == 0), so the
+// ragged-edge predicates fold away and the owner branches are warp-uniform.
 //
 // Warp roles and schedule per work item (planes indexed k = 0 .. L+1 from zs-1, L = ze-zs):
 //   owner warps (one per tile row):  rebuild own columns of plane k; for k >= 2 wait FULL(k),
@@ -213,7 +215,7 @@ __device__ __forceinline__ void nb_arrive(int id, int n) {
 // 1 + (k&1) / 3 + (k&1); a role can run at most one generation ahead on an id, so
 // consecutive generations never mix.  Counts are always the whole CTA (owner arrivals +
 // rim arrivals), so the rim work of the next plane overlaps the owners' emit.
-template <typename S, int TY, bool SPECIAL, bool BATCH>
+template <typename S, int TY, bool SPECIAL, bool BATCH, bool FULL>
 __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     step_kernel(const StepArgs *__restrict__ ga, const BatchArgs *__restrict__ ba, const int parity,
                 double *__restrict__ diag_part) {
@@ -279,11 +281,11 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         const int tile = item & 0xFFFFF, seg = item >> 20;
         const int tix = tile % tiles_x, tiy = tile / tiles_x;
         const int x0 = tix * TILE_X, y0 = tiy * TY;
-        const int w = min(TILE_X, nx - x0), h = min(TY, ny - y0);
+        const int w = FULL ? TILE_X : min(TILE_X, nx - x0), h = FULL ? TY : min(TY, ny - y0);
         const int zs = seg * lz, ze = min(zs + lz, nz);
         const int last = ze - zs + 1;  // last plane index k
         const int slot = (SPECIAL && tile_slot) ? tile_slot[tile] : -1;
-        const bool own = owner && tx < w && ty < h;
+        const bool own = owner && (FULL || (tx < w && ty < h));
         const int x = x0 + tx, y = y0 + ty;
         const int col = (ty + 1) * G::W + (tx + 1);
         // the column this thread loads and rebuilds: its own, or a rim column for rim warps
@@ -481,11 +483,11 @@ __global__ void diag_finalize_kernel(const double *__restrict__ part, int n, dou
 
 // Opt the kernel into its dynamic shared memory once per process (never inside a stream capture:
 // batched launches are prepared before their graphs are captured).
-template <typename S, int TY, bool SP, bool BATCH>
+template <typename S, int TY, bool SP, bool BATCH, bool FULL = false>
 cudaError_t configure_t() {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(step_kernel<S, TY, SP, BATCH>,
+        cudaError_t e = cudaFuncSetAttribute(step_kernel<S, TY, SP, BATCH, FULL>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, Geo<TY>::SMEM);
         if (e != cudaSuccess) return e;
         configured = true;
@@ -493,18 +495,30 @@ cudaError_t configure_t() {
     return cudaSuccess;
 }
 
-template <typename S, int TY, bool SP, bool BATCH>
+template <typename S, int TY, bool SP, bool BATCH, bool FULL = false>
 cudaError_t launch_t(const StepArgs *ga, const BatchArgs *ba, int parity, double *diag_part, int n_ctas,
                      cudaStream_t s) {
-    const cudaError_t e = configure_t<S, TY, SP, BATCH>();
+    const cudaError_t e = configure_t<S, TY, SP, BATCH, FULL>();
     if (e != cudaSuccess) return e;
-    step_kernel<S, TY, SP, BATCH><<<n_ctas, Geo<TY>::NTH, Geo<TY>::SMEM, s>>>(ga, ba, parity, diag_part);
+    step_kernel<S, TY, SP, BATCH, FULL><<<n_ctas, Geo<TY>::NTH, Geo<TY>::SMEM, s>>>(ga, ba, parity, diag_part);
     return cudaGetLastError();
 }
 
+// `full`: whole tiles only; used by the single-case bulk variant (the other variants keep the
+// ragged-edge predicates)
 template <typename S, bool SP, bool BATCH>
 cudaError_t launch_s(const StepArgs *ga, const BatchArgs *ba, int parity, double *diag_part, int n_ctas, int tile_y,
-                     cudaStream_t s) {
+                     bool full, cudaStream_t s) {
+    if constexpr (!SP && !BATCH) {
+        if (full) {
+            switch (tile_y) {
+                case 4: return launch_t<S, 4, false, false, true>(ga, ba, parity, diag_part, n_ctas, s);
+                case 8: return launch_t<S, 8, false, false, true>(ga, ba, parity, diag_part, n_ctas, s);
+                case 16: return launch_t<S, 16, false, false, true>(ga, ba, parity, diag_part, n_ctas, s);
+                default: return cudaErrorInvalidValue;
+            }
+        }
+    }
     switch (tile_y) {
         case 4: return launch_t<S, 4, SP, BATCH>(ga, ba, parity, diag_part, n_ctas, s);
         case 8: return launch_t<S, 8, SP, BATCH>(ga, ba, parity, diag_part, n_ctas, s);
@@ -516,8 +530,10 @@ cudaError_t launch_s(const StepArgs *ga, const BatchArgs *ba, int parity, double
 template <typename S, int TY>
 int occ_t() {
     int n = 0;
-    cudaFuncSetAttribute(step_kernel<S, TY, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, Geo<TY>::SMEM);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<S, TY, true, false>, Geo<TY>::NTH, Geo<TY>::SMEM) !=
+    cudaFuncSetAttribute(step_kernel<S, TY, true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         Geo<TY>::SMEM);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<S, TY, true, false, false>, Geo<TY>::NTH,
+                                                      Geo<TY>::SMEM) !=
         cudaSuccess)
         return 0;
     return n;
@@ -538,15 +554,18 @@ cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, bool speci
     const StepArgs *ga = l.ga;
     switch (storage) {
         case MRLBM_STORAGE_F32:
-            return special ? launch_s<float, true, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s)
-                           : launch_s<float, false, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s);
+            return special ? launch_s<float, true, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, false, s)
+                           : launch_s<float, false, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y,
+                                                           l.full_tiles, s);
         case MRLBM_STORAGE_F16:
-            return special ? launch_s<__half, true, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s)
-                           : launch_s<__half, false, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s);
+            return special ? launch_s<__half, true, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, false, s)
+                           : launch_s<__half, false, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y,
+                                                            l.full_tiles, s);
         case MRLBM_STORAGE_BF16:
-            return special
-                       ? launch_s<__nv_bfloat16, true, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s)
-                       : launch_s<__nv_bfloat16, false, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y, s);
+            return special ? launch_s<__nv_bfloat16, true, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y,
+                                                                  false, s)
+                           : launch_s<__nv_bfloat16, false, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas,
+                                                                   tile_y, l.full_tiles, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -580,14 +599,14 @@ cudaError_t launch_step_batch(const BatchArgs *ba, int parity, int storage, int 
                               cudaStream_t s) {
     switch (storage) {
         case MRLBM_STORAGE_F32:
-            return special ? launch_s<float, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s)
-                           : launch_s<float, false, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
+            return special ? launch_s<float, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, false, s)
+                           : launch_s<float, false, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, false, s);
         case MRLBM_STORAGE_F16:
-            return special ? launch_s<__half, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s)
-                           : launch_s<__half, false, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
+            return special ? launch_s<__half, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, false, s)
+                           : launch_s<__half, false, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, false, s);
         case MRLBM_STORAGE_BF16:
-            return special ? launch_s<__nv_bfloat16, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s)
-                           : launch_s<__nv_bfloat16, false, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, s);
+            return special ? launch_s<__nv_bfloat16, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, false, s)
+                           : launch_s<__nv_bfloat16, false, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, false, s);
         default: return cudaErrorInvalidValue;
     }
 }
