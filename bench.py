@@ -385,6 +385,10 @@ def run_ours(args):
         desc = cases.c2_taylor_green(args.n, STORAGE[storage])
         workload = f"taylor-green {args.n}^3 D3Q27, u0=0.05, Re=1600, {storage} moment storage"
         metric = metric_name(args.n)
+    sr = bool(args.stochastic_rounding) and storage != "f32"
+    if sr:
+        desc.stochastic_rounding = 1
+        workload += ", stochastic rounding"
     n_nodes = desc.nx * desc.ny * desc.nz
     stream = torch.cuda.Stream()  # a real stream handle: the library launches on it, events time it
     torch.cuda.set_stream(stream)
@@ -442,7 +446,8 @@ def run_ours(args):
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": storage, "data": "synthetic",
         "config": {"workload": workload,
-                   "storage": storage, "tile": list(info.tile), "ctas": int(info.reserved[0]),
+                   "storage": storage, "stochastic_rounding": sr, "tile": list(info.tile),
+                   "ctas": int(info.reserved[0]),
                    "l2": f"inputs larger than L2 ({n_nodes * 10 * (4 if storage == 'f32' else 2) / 1e6:.0f} MB "
                          f"per moment buffer vs 129 MB L2)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
@@ -453,7 +458,9 @@ def run_ours(args):
                      "traffic_source": "ncu dram__bytes_read+write per node (profiles/dram_traffic.txt) x nodes"},
         "e2e": {"value": e2e_value, "unit": "MLUPS", "h2d_bytes_per_step": hv.nbytes / e2e_steps,
                 "d2h_bytes_per_step": 16 + hv.nbytes / e2e_steps},
-        "gpu_launches": args.steps * (2 if cyl else 1),  # step kernel (+ wall kernel)
+        # per step: the step kernel; the cylinder adds the boundary-tile step kernel, the
+        # node-list kernel and the wall kernel; stochastic rounding adds its counter tick
+        "gpu_launches": args.steps * ((4 if cyl else 1) + sr),
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -472,6 +479,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f32", choices=list(STORAGE))
+    ap.add_argument("--stochastic-rounding", action="store_true",
+                    help="16-bit storage: round the time-step stores stochastically (cvt.rs)")
     ap.add_argument("--size", dest="n", type=int, default=256, help="TGV grid edge (n^3)")
     ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder", "batch", "c5"])
     ap.add_argument("--batch-cases", type=int, default=64)

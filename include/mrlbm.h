@@ -129,7 +129,10 @@ typedef struct mrlbm_case_desc {
     /* storage */
     int32_t storage;      /* MRLBM_STORAGE_*                                             */
     float storage_scale[3]; /* low-precision storage scales for (rho - rho0, u, m); 0 = auto */
-    int32_t reserved[16];
+    int32_t stochastic_rounding; /* FP16 / BF16 only: 1 rounds the time-step stores
+                                    stochastically (hardware cvt.rs with hashed random bits
+                                    per node, field pair and step) instead of to nearest     */
+    int32_t reserved[15];
 } mrlbm_case_desc;
 
 typedef struct mrlbm_info {
@@ -223,7 +226,7 @@ int mrlbm_write_pressure(mrlbm_handle *h, int32_t wall, const char *path);
  * it (the reference writes the line before it updates the mean).  append as for
  * mrlbm_write_forces. */
 int mrlbm_write_inlet_density(mrlbm_handle *h, const char *path, int32_t append);
-/* The grid_layout/*.dat node lists of the z = 0 slice, `x y z type index` per line, into the
+/* The node lists of the grid_layout directory for the z = 0 slice, `x y z type index` per line, into the
  * directory `dir` (write_geometry_files, cases/cylinder/cylinder_helpers.cuh:388-470):
  * inner, outer, bcfluid_inner, bcfluid_outer, bcsolid_inner, bcsolid_outer, solid, fluid,
  * others.  Host only; works on host-only handles. */

@@ -73,6 +73,7 @@ void free_all(mrlbm_handle *h) {
     f(h->d_tag);
     f(h->d_args);
     f(h->d_error);
+    f(h->d_sr_step);
     f(h->d_force_ring);
     f(h->d_diag_ring);
     f(h->d_diag_part);
@@ -100,6 +101,14 @@ int ensure_stage(mrlbm_handle *h, size_t bytes) {
     h->stage_bytes = 0;
     CK(h, cudaMalloc((void **)&h->d_stage, bytes));
     h->stage_bytes = bytes;
+    return MRLBM_OK;
+}
+
+int sync_sr_step(mrlbm_handle *h) {
+    if (!h->d_sr_step) return MRLBM_OK;
+    const uint32_t v = (uint32_t)h->step;
+    CK(h, cudaStreamSynchronize(h->stream));
+    CK(h, cudaMemcpy(h->d_sr_step, &v, sizeof(v), cudaMemcpyHostToDevice));
     return MRLBM_OK;
 }
 
@@ -324,6 +333,7 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
             h->diag_steps[slot] = it;
             ++h->diag_count;
         }
+        if (h->d_sr_step) CK(h, launch_sr_tick(h->d_sr_step, h->stream));
         h->parity ^= 1;
         ++h->step;
     }
@@ -378,7 +388,7 @@ int restore_state(mrlbm_handle *h, SavedState &st) {
     h->diag_count = st.diag_count;
     h->ps_start = st.ps_start;
     h->ps_end = st.ps_end;
-    return MRLBM_OK;
+    return sync_sr_step(h);
 }
 
 }  // namespace
@@ -616,6 +626,11 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     a.tag_in = h->d_tag;
     a.tag_out = h->d_tag ? h->d_tag + 256 : nullptr;
     a.error = h->d_error;
+    if (d.stochastic_rounding && d.storage != MRLBM_STORAGE_F32) {
+        CK(H, cudaMalloc((void **)&h->d_sr_step, sizeof(uint32_t)));
+        CK(H, cudaMemset(h->d_sr_step, 0, sizeof(uint32_t)));
+        a.sr_step = h->d_sr_step;
+    }
     CK(H, cudaMalloc((void **)&h->d_args, sizeof(StepArgs)));
     {
         int ty = 16, lz = 0;
@@ -698,7 +713,7 @@ int mrlbm_init(mrlbm_handle *h, int32_t kind, const double *params, int32_t n_pa
     std::fill(h->force_steps.begin(), h->force_steps.end(), -1);
     std::fill(h->diag_steps.begin(), h->diag_steps.end(), -1);
     h->initialized = true;
-    return MRLBM_OK;
+    return sync_sr_step(h);
 }
 
 int mrlbm_set_sampling(mrlbm_handle *h, int32_t force_every, int32_t diag_every) {
@@ -1057,6 +1072,9 @@ int batch_launch(mrlbm_batch *b, int parity, int force) {
     if (b->n_items_sp > 0) BCK(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
     BCK(launch_special_list_batch(b->d_ba, parity, force, b->storage, b->n_list_blocks, b->stream));
     BCK(launch_wall_batch(b->d_ba, parity, force, b->storage, b->n_wall_blocks, b->stream));
+    bool any_sr = false;
+    for (const mrlbm_handle *h : b->h) any_sr = any_sr || h->d_sr_step != nullptr;
+    if (any_sr) BCK(launch_sr_tick_cases(b->d_cases, (int)b->h.size(), b->stream));
     return MRLBM_OK;
 }
 

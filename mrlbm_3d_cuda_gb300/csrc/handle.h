@@ -66,6 +66,7 @@ struct mrlbm_handle {
     std::vector<int32_t> h_items, h_items_sp;  // host copies of the two work-item lists
     mrlbm_batch *batch = nullptr;   // owning batch, if any
     int *d_error = nullptr;
+    uint32_t *d_sr_step = nullptr;  // stochastic-rounding step counter (16-bit storage with it on)
     // sampling
     int force_every = 0, diag_every = 0;
     double *d_force_ring = nullptr, *d_diag_ring = nullptr, *d_diag_part = nullptr;
@@ -119,6 +120,8 @@ int fail(mrlbm_handle *h, int code, const std::string &msg);
 int cuda_fail(mrlbm_handle *h, cudaError_t e, const char *what);
 // Device staging buffer of at least `bytes` (FP32 host-layout conversions).
 int ensure_stage(mrlbm_handle *h, size_t bytes);
+// Set the stochastic-rounding step counter to the handle's step (after init, load, restore).
+int sync_sr_step(mrlbm_handle *h);
 }  // namespace mrlbm
 
 #define CK(h, call)                                                    \

@@ -71,6 +71,9 @@ struct StepArgs {
     float *popbuf = nullptr;              // [27][n_list_pop]
     const int32_t *row_base = nullptr;    // [slot][z][tile row]: first list entry of the row
     int *work_counter = nullptr;          // work items claimed beyond the first gridDim.x (zeroed per launch)
+    // stochastic rounding of 16-bit stores: the step counter that seeds the random bits
+    // (null: round to nearest)
+    const uint32_t *sr_step = nullptr;
 };
 
 // Several independent cases advanced together: one step-kernel launch over the work items of
@@ -132,6 +135,9 @@ struct InitArgs {
     StorageScale sc;
 };
 cudaError_t launch_init(const InitArgs &a, int storage, cudaStream_t s);
+// Advance the stochastic-rounding step counter(s) after a step.
+cudaError_t launch_sr_tick(uint32_t *ctr, cudaStream_t s);
+cudaError_t launch_sr_tick_cases(const StepArgs *const *cases, int n, cudaStream_t s);
 
 // Convert between device storage and an FP32 staging buffer (lexicographic or reference
 // tiled layout).  dir = 0: storage -> f32, 1: f32 -> storage (written to dst_a and dst_b).

@@ -112,7 +112,7 @@ int mrlbm_checkpoint_load(mrlbm_handle *h, const char *path) {
     const int rc = mrlbm_set_moments(h, MRLBM_FIELD_ALL, MRLBM_LAYOUT_REF_TILED, mom.data(), mom.size());
     if (rc) return rc;
     h->step = iter;
-    return MRLBM_OK;
+    return sync_sr_step(h);
 }
 
 int mrlbm_write_vti(mrlbm_handle *h, const char *path) {

@@ -172,7 +172,13 @@ __global__ void __launch_bounds__(kListThreads)
         const int slot = a.tile_slot[ty * a.tiles_x + tx];
         Mom m;
         const int code = special_node<S>(a, parity, force != 0, w, f, x, y, z, slot, tx * TILE_X, ty * a.tile_y, m);
-        if (code) store_mom<S>(dst, aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S)), m, a.rho0, a.sc);
+        if (code) {
+            const int64_t ai = aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S));
+            if (sizeof(S) == 2 && a.sr_step)
+                store_mom_sr<S>(dst, ai, m, a.rho0, a.sc, sr_key(sr_step_seed(*a.sr_step), x, y, z, a.nx, a.ny));
+            else
+                store_mom<S>(dst, ai, m, a.rho0, a.sc);
+        }
         if (code == 2 && diag_part) {
             dm += (double)(m.rho - a.rho0);
             de += 0.5 * (double)(m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);

@@ -234,6 +234,8 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     float omega = 1.f, rho0 = 1.f;
     StorageScale sc;
     int64_t plane = 0, zst = 0;  // lexicographic plane (node words), storage elements per z plane
+    bool sr_on = false;          // stochastic rounding of 16-bit stores
+    uint32_t sr_seed = 0u;
     auto load_case = [&](const StepArgs *__restrict__ c) {
         src = (const S *)c->m[parity];
         dst = (S *)c->m[parity ^ 1];
@@ -253,6 +255,10 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         sc = c->sc;
         plane = (int64_t)nx * ny;
         zst = (int64_t)ny * nxb * 10 * kXBlock;
+        if constexpr (sizeof(S) == 2) {
+            sr_on = c->sr_step != nullptr;
+            sr_seed = sr_on ? sr_step_seed(*c->sr_step) : 0u;
+        }
     };
     if constexpr (!BATCH) load_case(ga);
     const int n_items = BATCH ? ba->n_items : ga->n_items;
@@ -381,7 +387,10 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                                 de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
                             }
                             collide(m, omega);
-                            store_mom<S>(dst, ai, m, rho0, sc);
+                            if (sizeof(S) == 2 && sr_on)
+                                store_mom_sr<S>(dst, ai, m, rho0, sc, sr_key(sr_seed, x, y, z, nx, ny));
+                            else
+                                store_mom<S>(dst, ai, m, rho0, sc);
                         } else if (exp) {
                             // non-bulk node: hand its pulled populations to the node-list kernel
                             float fw[27];

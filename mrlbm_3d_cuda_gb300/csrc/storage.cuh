@@ -87,6 +87,40 @@ __device__ __forceinline__ uint32_t pair_from_f<__nv_bfloat16>(float a, float b)
     return w;
 }
 
+// Stochastic rounding of two floats to one packed 16-bit pair with Blackwell's cvt.rs:
+// `lo` goes to the lower half (lower address), `hi` to the upper half; `rbits` are the
+// random bits that decide each rounding direction.
+template <typename S>
+__device__ __forceinline__ uint32_t pair_from_f_sr(float lo, float hi, uint32_t rbits);
+template <>
+__device__ __forceinline__ uint32_t pair_from_f_sr<__half>(float lo, float hi, uint32_t rbits) {
+    uint32_t d;
+    asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+    return d;
+}
+template <>
+__device__ __forceinline__ uint32_t pair_from_f_sr<__nv_bfloat16>(float lo, float hi, uint32_t rbits) {
+    uint32_t d;
+    asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+    return d;
+}
+
+// 32-bit integer hash ("lowbias32" from C. Wellons' hash prospector): avalanching, so the
+// node index, field pair and step number give independent-looking random bits.
+__host__ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+// Random-bit key of node (x, y, z) at the step with seed mix32(step): one per node and step.
+__device__ __forceinline__ uint32_t sr_key(uint32_t step_seed, int x, int y, int z, int nx, int ny) {
+    return mix32((((uint32_t)z * (uint32_t)ny + (uint32_t)y) * (uint32_t)nx + (uint32_t)x) ^ step_seed);
+}
+__device__ __forceinline__ uint32_t sr_step_seed(uint32_t step) { return mix32(step * 0x9e3779b9u + 0x632be5abu); }
+
 // `ai` is the element index of field 0 of a node (aos_index); field k sits at
 // ai + field_offset(k): 32 k for FP32, 64 (k / 2) + k % 2 for FP16 / BF16 (ai is even there).
 template <typename S>
@@ -135,6 +169,23 @@ __device__ __forceinline__ void store_mom(S *__restrict__ base, int64_t ai, cons
         w[2 * kXBlock] = pair_from_f<S>(m.mxx * sc.s[2], m.myy * sc.s[2]);
         w[3 * kXBlock] = pair_from_f<S>(m.mzz * sc.s[2], m.mxy * sc.s[2]);
         w[4 * kXBlock] = pair_from_f<S>(m.mxz * sc.s[2], m.myz * sc.s[2]);
+    }
+}
+
+// store_mom with stochastic rounding of the 16-bit pairs (random bits from `key`, one hash per
+// pair); FP32 storage has nothing to round
+template <typename S>
+__device__ __forceinline__ void store_mom_sr(S *__restrict__ base, int64_t ai, const Mom &m, float rho0,
+                                             const StorageScale &sc, uint32_t key) {
+    if constexpr (std::is_same<S, float>::value) {
+        store_mom<S>(base, ai, m, rho0, sc);
+    } else {
+        uint32_t *w = reinterpret_cast<uint32_t *>(base + ai);
+        w[0 * kXBlock] = pair_from_f_sr<S>((m.rho - rho0) * sc.s[0], m.ux * sc.s[1], mix32(key));
+        w[1 * kXBlock] = pair_from_f_sr<S>(m.uy * sc.s[1], m.uz * sc.s[1], mix32(key + 0x9e3779b9u));
+        w[2 * kXBlock] = pair_from_f_sr<S>(m.mxx * sc.s[2], m.myy * sc.s[2], mix32(key + 0x3c6ef372u));
+        w[3 * kXBlock] = pair_from_f_sr<S>(m.mzz * sc.s[2], m.mxy * sc.s[2], mix32(key + 0xdaa66d2bu));
+        w[4 * kXBlock] = pair_from_f_sr<S>(m.mxz * sc.s[2], m.myz * sc.s[2], mix32(key + 0x78dde6e4u));
     }
 }
 

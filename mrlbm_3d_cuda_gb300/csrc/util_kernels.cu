@@ -113,7 +113,26 @@ __global__ void convert_kernel(const S *src, S *dst_a, S *dst_b, float *f32, uin
     }
 }
 
+// One step further along the stochastic-rounding random sequence: the step counter of one
+// case, or of every case of a batch that rounds stochastically.
+__global__ void sr_tick_kernel(uint32_t *ctr) { ++*ctr; }
+__global__ void sr_tick_cases_kernel(const StepArgs *const *cases, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && cases[i]->sr_step) ++*const_cast<uint32_t *>(cases[i]->sr_step);
+}
+
 }  // namespace
+
+cudaError_t launch_sr_tick(uint32_t *ctr, cudaStream_t s) {
+    sr_tick_kernel<<<1, 1, 0, s>>>(ctr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sr_tick_cases(const StepArgs *const *cases, int n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    sr_tick_cases_kernel<<<(n + 127) / 128, 128, 0, s>>>(cases, n);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_init(const InitArgs &a, int storage, cudaStream_t s) {
     const int64_t n = (int64_t)a.nx * a.ny * a.nz;

@@ -208,7 +208,12 @@ __global__ void __launch_bounds__(128)
                 double fin[4] = {0.0, 0.0, 0.0, 0.0}, fo[4];
                 if (force) masked_momentum64(inm, m, fin);
                 collide(m, a.omega);
-                store_mom<S>((S *)a.m[parity ^ 1], aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S)), m, a.rho0, a.sc);
+                const int64_t ai = aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S));
+                if (sizeof(S) == 2 && a.sr_step)
+                    store_mom_sr<S>((S *)a.m[parity ^ 1], ai, m, a.rho0, a.sc,
+                                    sr_key(sr_step_seed(*a.sr_step), x, y, z, a.nx, a.ny));
+                else
+                    store_mom<S>((S *)a.m[parity ^ 1], ai, m, a.rho0, a.sc);
                 if (force) {
                     masked_momentum64(outm, m, fo);
                     const double fx = fin[0] - fo[0], fy = fin[1] - fo[1];

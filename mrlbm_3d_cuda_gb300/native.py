@@ -50,7 +50,8 @@ class CaseDesc(C.Structure):
         ("convective_outlet", C.c_int32), ("neumann_current_update", C.c_int32),
         ("storage", C.c_int32),
         ("storage_scale", C.c_float * 3),
-        ("reserved", C.c_int32 * 16),
+        ("stochastic_rounding", C.c_int32),
+        ("reserved", C.c_int32 * 15),
     ]
 
 

@@ -12,7 +12,9 @@ step must satisfy at every size.
   rate comes out 13.5% low (measured on a GB300).  The likely cause: at this grid size the
   viscous stress is about 1% of the stored m_ab ~ u_a u_b, so FP16's 2^-11 relative rounding
   of m is a few percent of the stress, and on a smooth field the rounding errors are spatially
-  correlated rather than averaging out.  The FP16 bound is 20%.
+  correlated rather than averaging out.  The FP16 bound is 20%.  With stochastic rounding the
+  rounding errors are independent and FP16 decays like FP32 (measured +0.19%, FP32 +0.23%):
+  bound 3%.
 """
 from __future__ import annotations
 
@@ -47,15 +49,17 @@ def shifted_pair(desc, init, params, steps):
     return same, diag
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16"])
+@pytest.mark.parametrize("storage", ["f32", "f16", "f16sr"])
 def test_taylor_green_256_shift_invariance_conservation_decay(cuda_device, storage):
     from mrlbm_3d_cuda_gb300 import cases
     from mrlbm_3d_cuda_gb300 import native as N
     st = N.STORAGE_F32 if storage == "f32" else N.STORAGE_F16
     desc = cases.periodic_box(256, u0=0.05, re=100.0, storage=st)
+    desc.stochastic_rounding = int(storage == "f16sr")
     steps = 250
     same, diag = shifted_pair(desc, N.INIT_TAYLOR_GREEN, cases.tgv_params(desc), steps)
-    assert same, "the step does not commute with a periodic shift"
+    # stochastic rounding keys its random bits on the absolute node index: no shift symmetry
+    assert same or storage == "f16sr", "the step does not commute with a periodic shift"
     n = 256 ** 3
     mass, energy = diag[:, 0], diag[:, 1]
     # FP32 weights sum to 1 within a few ulp: the mean density may drift ~3e-7 per step
@@ -63,7 +67,7 @@ def test_taylor_green_256_shift_invariance_conservation_decay(cuda_device, stora
     nu = (1.0 / desc.omega - 0.5) / 3.0
     want = 2.0 * nu * 3.0 / desc.length ** 2
     rate = -math.log(energy[-1] / energy[50]) / (len(energy) - 1 - 50)
-    assert abs(rate - want) / want < (0.03 if storage == "f32" else 0.20), (rate, want)
+    assert abs(rate - want) / want < (0.20 if storage == "f16" else 0.03), (rate, want)
 
 
 def test_largest_single_gpu_grid_shift_invariance(cuda_device):
