@@ -313,8 +313,12 @@ def run_c5(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     stats, value, ms_step, clocks = {}, None, None, None
-    for st in ("f16", "f32"):
+    runs = args.c5_runs.split(",")
+    workload = ""  # described by the FP16 run
+    sr = bool(args.stochastic_rounding)
+    for st in runs:
         desc = cases.c5_turbulent_cylinder(STORAGE[st], re=args.re)
+        desc.stochastic_rounding = int(sr and st != "f32")
         sim = Simulation(desc, init=False)
         sim.set_stream(stream.cuda_stream)
         if args.c5_init == "noisy":
@@ -346,9 +350,11 @@ def run_c5(args):
             n_nodes = desc.nx * desc.ny * desc.nz
             value, ms_step, clocks = replica_value(n_nodes, ms_done, ms * 1e-3, 1), ms / ms_done, clk.summary()
             workload = (f"cylinder {desc.nx}x{desc.ny}x{desc.nz}, D={desc.d_wall[0]:.0f}, Re={args.re:g}, u=0.05, "
-                        f"start: {'uniform +1% noise' if args.c5_init == 'noisy' else 'rest'}, tau={1 / desc.omega:.5f}")
+                        f"start: {'uniform +1% noise' if args.c5_init == 'noisy' else 'rest'}, tau={1 / desc.omega:.5f}"
+                        + (", FP16 stochastic rounding" if sr else ""))
         sim.close()
-    (cd16, cl16, st16, div16), (cd32, cl32, st32, div32) = stats["f16"], stats["f32"]
+    nan4 = (float("nan"),) * 3 + (None,)
+    (cd16, cl16, st16, div16), (cd32, cl32, st32, div32) = stats.get("f16", nan4), stats.get("f32", nan4)
     line = {
         "metric": "MLUPS (D3Q27 MR-LBM, 1024x512x256 cylinder, FP16 storage)", "value": value,
         "unit": "MLUPS", "n_gpus": 1, "steps": args.steps, "warmup": 0, "ms_per_step": ms_step,
@@ -358,7 +364,7 @@ def run_c5(args):
                    "f32": {"cd": cd32, "cl_rms": cl32, "st": st32, "diverged_at_step": div32},
                    "cd_rel_err": cd16 / cd32 - 1, "cl_rms_rel_err": cl16 / cl32 - 1, "st_rel_err": st16 / st32 - 1,
                    "statistics": "second half of the run; St from the Cl spectrum peak"},
-        "gpu_launches": 3 * args.steps, "clocks": clocks,
+        "gpu_launches": (3 + sr) * args.steps, "clocks": clocks,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -486,6 +492,7 @@ def main():
     ap.add_argument("--batch-cases", type=int, default=64)
     ap.add_argument("--re", type=float, default=3900.0, help="Reynolds number of the c5 workload")
     ap.add_argument("--c5-init", default="noisy", choices=["noisy", "rest"])
+    ap.add_argument("--c5-runs", default="f16,f32", help="storage runs of the c5 workload (f16 first: its speed is the value)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--diameter", type=int, default=16)
     ap.add_argument("--ref-slab", type=int, default=8)

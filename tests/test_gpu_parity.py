@@ -107,6 +107,17 @@ def test_non_multiple_of_tile_grid(cuda_device):
     assert_fields(res, 0.05, strict=True)
 
 
+@pytest.mark.parametrize("shape", [(8, 8, 4), (8, 24, 4), (72, 8, 12)])
+def test_smallest_grids(cuda_device, shape):
+    """Grids at the reference's minimum granularity (multiples of 8, 8, 4): one partial tile,
+    a one-plane-deep z segment per item, a single x-block."""
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    desc = cases.periodic_box(*shape, u0=0.04, re=100.0)
+    res = run_pair(desc, 10, N.INIT_NOISY_UNIFORM, (0.03, 0.01, -0.02, 0.3, 7), fp64=False)
+    assert_fields(res, 0.05, strict=True)
+
+
 def test_channel_short_run_strict(cuda_device):
     from mrlbm_3d_cuda_gb300 import cases
     from mrlbm_3d_cuda_gb300 import native as N
