@@ -32,13 +32,16 @@ struct Mom {
 // p0 = 1 - 1.5 tr(m).  Every FMA is written out (__fmaf_rn) and every product that must not
 // fuse goes through __fmul_rn: the owner and the rim copies of this function keep different
 // subsets of the populations, and free contraction made the two round differently.
-__device__ __forceinline__ void reconstruct(const Mom &m, float f[27]) {
+// The Hermite factors 3 (u), 1.5, 4.5 and 9 (m) are parameters so that moments stored with a
+// scale (16-bit storage) can be rebuilt without unscaling them first: pass 3 / s_u, 1.5 / s_m,
+// 4.5 / s_m and 9 / s_m with the stored u and m.
+__device__ __forceinline__ void reconstruct_h(const Mom &m, float h3, float h15, float h45, float h9, float f[27]) {
     const float t = __fadd_rn(__fadd_rn(m.mxx, m.myy), m.mzz);
-    const float p0 = __fmaf_rn(-1.5f, t, 1.0f);
-    const float ax = __fmaf_rn(4.5f, m.mxx, p0), ay = __fmaf_rn(4.5f, m.myy, p0), az = __fmaf_rn(4.5f, m.mzz, p0);
+    const float p0 = __fmaf_rn(-h15, t, 1.0f);
+    const float ax = __fmaf_rn(h45, m.mxx, p0), ay = __fmaf_rn(h45, m.myy, p0), az = __fmaf_rn(h45, m.mzz, p0);
     const float r1 = __fmul_rn(m.rho, kW1), r2 = __fmul_rn(m.rho, kW2), r3 = __fmul_rn(m.rho, kW3);
-    const float q1 = __fmul_rn(3.0f, r1), q2 = __fmul_rn(3.0f, r2), q3 = __fmul_rn(3.0f, r3);
-    const float n2 = __fmul_rn(9.0f, r2), n3 = __fmul_rn(9.0f, r3);
+    const float q1 = __fmul_rn(h3, r1), q2 = __fmul_rn(h3, r2), q3 = __fmul_rn(h3, r3);
+    const float n2 = __fmul_rn(h9, r2), n3 = __fmul_rn(h9, r3);
     f[0] = __fmul_rn(__fmul_rn(m.rho, kW0), p0);
     {
         const float ex = __fmul_rn(r1, ax), ey = __fmul_rn(r1, ay), ez = __fmul_rn(r1, az);
@@ -51,7 +54,7 @@ __device__ __forceinline__ void reconstruct(const Mom &m, float f[27]) {
     }
     const float upp = __fadd_rn(m.ux, m.uy), upm = __fsub_rn(m.ux, m.uy);
     {
-        const float b = __fmul_rn(r2, __fmaf_rn(4.5f, m.myy, ax));
+        const float b = __fmul_rn(r2, __fmaf_rn(h45, m.myy, ax));
         const float cp = __fmaf_rn(n2, m.mxy, b), cm = __fmaf_rn(-n2, m.mxy, b);
         f[7] = __fmaf_rn(q2, upp, cp);
         f[8] = __fmaf_rn(-q2, upp, cp);
@@ -59,7 +62,7 @@ __device__ __forceinline__ void reconstruct(const Mom &m, float f[27]) {
         f[14] = __fmaf_rn(-q2, upm, cm);
     }
     {
-        const float b = __fmul_rn(r2, __fmaf_rn(4.5f, m.mzz, ax));
+        const float b = __fmul_rn(r2, __fmaf_rn(h45, m.mzz, ax));
         const float cp = __fmaf_rn(n2, m.mxz, b), cm = __fmaf_rn(-n2, m.mxz, b);
         const float sp = __fadd_rn(m.ux, m.uz), sm = __fsub_rn(m.ux, m.uz);
         f[9] = __fmaf_rn(q2, sp, cp);
@@ -68,7 +71,7 @@ __device__ __forceinline__ void reconstruct(const Mom &m, float f[27]) {
         f[16] = __fmaf_rn(-q2, sm, cm);
     }
     {
-        const float b = __fmul_rn(r2, __fmaf_rn(4.5f, m.mzz, ay));
+        const float b = __fmul_rn(r2, __fmaf_rn(h45, m.mzz, ay));
         const float cp = __fmaf_rn(n2, m.myz, b), cm = __fmaf_rn(-n2, m.myz, b);
         const float sp = __fadd_rn(m.uy, m.uz), sm = __fsub_rn(m.uy, m.uz);
         f[11] = __fmaf_rn(q2, sp, cp);
@@ -77,7 +80,7 @@ __device__ __forceinline__ void reconstruct(const Mom &m, float f[27]) {
         f[18] = __fmaf_rn(-q2, sm, cm);
     }
     {
-        const float c0 = __fmul_rn(r3, __fmaf_rn(4.5f, t, p0));
+        const float c0 = __fmul_rn(r3, __fmaf_rn(h45, t, p0));
         const float a = __fadd_rn(m.mxy, m.mxz), b = __fsub_rn(m.mxy, m.mxz);
         const float e1 = __fmaf_rn(n3, __fadd_rn(a, m.myz), c0), e2 = __fmaf_rn(n3, __fsub_rn(b, m.myz), c0);
         const float e3 = __fmaf_rn(-n3, __fadd_rn(b, m.myz), c0), e4 = __fmaf_rn(-n3, __fsub_rn(a, m.myz), c0);
@@ -93,6 +96,8 @@ __device__ __forceinline__ void reconstruct(const Mom &m, float f[27]) {
         f[25] = __fmaf_rn(-q3, s4, e4);
     }
 }
+
+__device__ __forceinline__ void reconstruct(const Mom &m, float f[27]) { reconstruct_h(m, 3.0f, 1.5f, 4.5f, 9.0f, f); }
 
 // rho = sum f, u = sum c f / rho, m_ab = sum c_a c_b f / rho - cs2 delta_ab, via the 13
 // opposite-pair sums e and differences d.
@@ -137,9 +142,11 @@ __device__ __forceinline__ void evaluate(const float f[27], Mom &m) {
 // m_ab <- (1 - omega) m_ab + omega u_a u_b; rho and u are collision invariants.  The rounding order is spelled out with
 // intrinsics: `a*b + c*d` has two possible FMA contractions, and leaving the choice to the
 // compiler let different kernel instantiations (tile heights) round differently.
-__device__ __forceinline__ void collide(Mom &m, float omega) {
+// omega_u = omega s_m / s_u^2 collides moments held with storage scales (u s_u, m s_m);
+// omega_u = omega for physical moments.
+__device__ __forceinline__ void collide_h(Mom &m, float omega, float omega_u) {
     const float om1 = 1.0f - omega;
-    const float wx = __fmul_rn(omega, m.ux), wy = __fmul_rn(omega, m.uy), wz = __fmul_rn(omega, m.uz);
+    const float wx = __fmul_rn(omega_u, m.ux), wy = __fmul_rn(omega_u, m.uy), wz = __fmul_rn(omega_u, m.uz);
     m.mxx = __fmaf_rn(wx, m.ux, __fmul_rn(om1, m.mxx));
     m.myy = __fmaf_rn(wy, m.uy, __fmul_rn(om1, m.myy));
     m.mzz = __fmaf_rn(wz, m.uz, __fmul_rn(om1, m.mzz));
@@ -147,6 +154,8 @@ __device__ __forceinline__ void collide(Mom &m, float omega) {
     m.mxz = __fmaf_rn(wx, m.uz, __fmul_rn(om1, m.mxz));
     m.myz = __fmaf_rn(wy, m.uz, __fmul_rn(om1, m.myz));
 }
+
+__device__ __forceinline__ void collide(Mom &m, float omega) { collide_h(m, omega, omega); }
 
 // ---------------------------------------------------------------------------------------
 // Boundary closures (rare nodes; kept out of the bulk path with __noinline__ callers).

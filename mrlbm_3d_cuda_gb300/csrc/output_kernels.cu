@@ -49,9 +49,9 @@ __global__ void halo_export_kernel(const StepArgs *__restrict__ ga, int parity, 
     if (!(wx || ex || sy || ny_ || bz || fz)) return;
     const int64_t gx = a.nx / kBX, gy = a.ny / kBY;
     const int64_t block = x / kBX + gx * (y / kBY + gy * (z / kBZ));
-    const Mom m = load_mom<S>((const S *)a.m[parity], aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S)), a.rho0, a.sc);
-    float f[27];
-    reconstruct(m, f);
+    float raw[10], f[27];
+    load_raw<S>((const S *)a.m[parity], aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S)), raw);
+    rebuild<S>(raw, a.rho0, a.sc, f);
 #pragma unroll
     for (int j = 0; j < kQF; ++j) {
         const int64_t px = ty + kBY * (tz + kBZ * (j + kQF * block));

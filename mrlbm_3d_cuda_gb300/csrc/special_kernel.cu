@@ -52,9 +52,9 @@ __device__ __noinline__ Mom pulled_rho_u(const StepArgs &a, const S *__restrict_
 #pragma unroll 1
     for (int q = 0; q < 27; ++q) {
         const int xs = (x - cxq(q) + a.nx) % a.nx, ys = (y - cyq(q) + a.ny) % a.ny, zs = (z - czq(q) + a.nz) % a.nz;
-        const Mom mq = load_mom<S>(src, aos_index(xs, ys, zs, a.nxb, a.ny, (int)sizeof(S)), a.rho0, a.sc);
-        float g[27];
-        reconstruct(mq, g);
+        float raw[10], g[27];
+        load_raw<S>(src, aos_index(xs, ys, zs, a.nxb, a.ny, (int)sizeof(S)), raw);
+        rebuild<S>(raw, a.rho0, a.sc, g);
         f[q] = g[q];
     }
     return rho_u_of(f);

@@ -64,11 +64,12 @@ constexpr bool need_dir(int q, int rcx, int rcy) {
 
 // Rebuild the populations of one rim column and store the ones the tile pulls from it
 // (rcx, rcy: the c_x / c_y a population must have to enter the tile from this rim side).
-template <int RCX, int RCY, int TY>
-__device__ __forceinline__ void rim_store(const Mom &m, float *up, float *fl, float *dn, int col) {
+template <typename S, int RCX, int RCY, int TY>
+__device__ __forceinline__ void rim_store(const float raw[10], float rho0, const StorageScale &sc, float *up,
+                                          float *fl, float *dn, int col) {
     constexpr int NC = Geo<TY>::NCOL;
     float f[27];
-    reconstruct(m, f);
+    rebuild<S>(raw, rho0, sc, f);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         if (need_dir(hUp(j), RCX, RCY)) up[j * NC + col] = f[hUp(j)];
@@ -116,9 +117,10 @@ __device__ __forceinline__ ClassSums class_sums(float mm, float m0, float mp, fl
 
 // Gather the pulled populations of the owner node and evaluate its moments on the fly,
 // class by class (c_z = +1 from plane z-1, 0 from z, -1 from z+1).
-template <int TY>
+// SCALED: u and the second moments come out multiplied by the storage scales su and sm.
+template <int TY, bool SCALED = false>
 __device__ __forceinline__ void gather_evaluate(const float *up, const float *fl, const float *dn, int col, float f0,
-                                                float f5, float f6, Mom &m) {
+                                                float f5, float f6, Mom &m, float su = 1.0f, float sm = 1.0f) {
 #define MRLBM_P(q) pull<q, TY>(up, fl, dn, col)
     // c_z = +1: (cx,cy) = (-1,-1) 22, (-1,0) 16, (-1,1) 25, (0,-1) 18, (0,0) 5, (0,1) 11, (1,-1) 23, (1,0) 9, (1,1) 19
     const ClassSums u = class_sums(MRLBM_P(22), MRLBM_P(16), MRLBM_P(25), MRLBM_P(18), f5, MRLBM_P(11), MRLBM_P(23),
@@ -132,16 +134,18 @@ __device__ __forceinline__ void gather_evaluate(const float *up, const float *fl
 #undef MRLBM_P
     const float rho = (u.s0 + c.s0) + d.s0;
     const float inv = 1.0f / rho;
+    const float iu = SCALED ? __fmul_rn(inv, su) : inv, im = SCALED ? __fmul_rn(inv, sm) : inv;
+    const float cs = SCALED ? __fmul_rn(-kCs2, sm) : -kCs2;
     m.rho = rho;
-    m.ux = ((u.sx + c.sx) + d.sx) * inv;
-    m.uy = ((u.sy + c.sy) + d.sy) * inv;
-    m.uz = (u.s0 - d.s0) * inv;
-    m.mxx = __fmaf_rn((u.sxx + c.sxx) + d.sxx, inv, -kCs2);
-    m.myy = __fmaf_rn((u.syy + c.syy) + d.syy, inv, -kCs2);
-    m.mzz = __fmaf_rn(u.s0 + d.s0, inv, -kCs2);
-    m.mxy = ((u.sxy + c.sxy) + d.sxy) * inv;
-    m.mxz = (u.sx - d.sx) * inv;
-    m.myz = (u.sy - d.sy) * inv;
+    m.ux = ((u.sx + c.sx) + d.sx) * iu;
+    m.uy = ((u.sy + c.sy) + d.sy) * iu;
+    m.uz = (u.s0 - d.s0) * iu;
+    m.mxx = __fmaf_rn((u.sxx + c.sxx) + d.sxx, im, cs);
+    m.myy = __fmaf_rn((u.syy + c.syy) + d.syy, im, cs);
+    m.mzz = __fmaf_rn(u.s0 + d.s0, im, cs);
+    m.mxy = ((u.sxy + c.sxy) + d.sxy) * im;
+    m.mxz = (u.sx - d.sx) * im;
+    m.myz = (u.sy - d.sy) * im;
 }
 
 template <int TY>
@@ -162,9 +166,8 @@ __device__ __forceinline__ void gather_all(const float *up, const float *fl, con
 template <typename S, int TY>
 __device__ __forceinline__ void arrive_own(const float raw[10], float rho0, const StorageScale &sc, float *up,
                                            float *fl, float *dn, int col, float &c0, float &c5, float &c6) {
-    const Mom m = decode<S>(raw, rho0, sc);
     float f[27];
-    reconstruct(m, f);
+    rebuild<S>(raw, rho0, sc, f);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         up[j * Geo<TY>::NCOL + col] = f[hUp(j)];
@@ -179,16 +182,15 @@ __device__ __forceinline__ void arrive_own(const float raw[10], float rho0, cons
 template <typename S, int TY>
 __device__ __forceinline__ void arrive_rim(const float raw[10], float rho0, const StorageScale &sc, int side, float *up,
                                            float *fl, float *dn, int rcol) {
-    const Mom m = decode<S>(raw, rho0, sc);
     switch (side) {
-        case 0: rim_store<0, 1, TY>(m, up, fl, dn, rcol); break;
-        case 1: rim_store<0, -1, TY>(m, up, fl, dn, rcol); break;
-        case 2: rim_store<1, 0, TY>(m, up, fl, dn, rcol); break;
-        case 3: rim_store<-1, 0, TY>(m, up, fl, dn, rcol); break;
-        case 4: rim_store<1, 1, TY>(m, up, fl, dn, rcol); break;
-        case 5: rim_store<-1, 1, TY>(m, up, fl, dn, rcol); break;
-        case 6: rim_store<1, -1, TY>(m, up, fl, dn, rcol); break;
-        default: rim_store<-1, -1, TY>(m, up, fl, dn, rcol); break;
+        case 0: rim_store<S, 0, 1, TY>(raw, rho0, sc, up, fl, dn, rcol); break;
+        case 1: rim_store<S, 0, -1, TY>(raw, rho0, sc, up, fl, dn, rcol); break;
+        case 2: rim_store<S, 1, 0, TY>(raw, rho0, sc, up, fl, dn, rcol); break;
+        case 3: rim_store<S, -1, 0, TY>(raw, rho0, sc, up, fl, dn, rcol); break;
+        case 4: rim_store<S, 1, 1, TY>(raw, rho0, sc, up, fl, dn, rcol); break;
+        case 5: rim_store<S, -1, 1, TY>(raw, rho0, sc, up, fl, dn, rcol); break;
+        case 6: rim_store<S, 1, -1, TY>(raw, rho0, sc, up, fl, dn, rcol); break;
+        default: rim_store<S, -1, -1, TY>(raw, rho0, sc, up, fl, dn, rcol); break;
     }
 }
 
@@ -236,6 +238,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     int64_t plane = 0, zst = 0;  // lexicographic plane (node words), storage elements per z plane
     bool sr_on = false;          // stochastic rounding of 16-bit stores
     uint32_t sr_seed = 0u;
+    float omega_u = 1.f;         // omega s_m / s_u^2: collision of scaled 16-bit moments
     auto load_case = [&](const StepArgs *__restrict__ c) {
         src = (const S *)c->m[parity];
         dst = (S *)c->m[parity ^ 1];
@@ -258,6 +261,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         if constexpr (sizeof(S) == 2) {
             sr_on = c->sr_step != nullptr;
             sr_seed = sr_on ? sr_step_seed(*c->sr_step) : 0u;
+            omega_u = c->omega * (c->sc.s[2] * (c->sc.is[1] * c->sc.is[1]));
         }
     };
     if constexpr (!BATCH) load_case(ga);
@@ -381,16 +385,28 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                         }
                         if (wd == 0u) {
                             Mom m;
-                            gather_evaluate<TY>(eup, efl, dn, col, p0, pp5, c6, m);
-                            if (diag) {
-                                dm += m.rho - rho0;
-                                de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
-                            }
-                            collide(m, omega);
-                            if (sizeof(S) == 2 && sr_on)
-                                store_mom_sr<S>(dst, ai, m, rho0, sc, sr_key(sr_seed, x, y, z, nx, ny));
-                            else
+                            if constexpr (std::is_same<S, float>::value) {
+                                gather_evaluate<TY>(eup, efl, dn, col, p0, pp5, c6, m);
+                                if (diag) {
+                                    dm += m.rho - rho0;
+                                    de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
+                                }
+                                collide(m, omega);
                                 store_mom<S>(dst, ai, m, rho0, sc);
+                            } else {
+                                // u and m come out with their storage scales: no unscaling on
+                                // the way in (rebuild) and no scaling on the way out
+                                gather_evaluate<TY, true>(eup, efl, dn, col, p0, pp5, c6, m, sc.s[1], sc.s[2]);
+                                if (diag) {
+                                    dm += m.rho - rho0;
+                                    de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz) * (sc.is[1] * sc.is[1]);
+                                }
+                                collide_h(m, omega, omega_u);
+                                if (sr_on)
+                                    store_scaled_sr<S>(dst, ai, m, rho0, sc, sr_key(sr_seed, x, y, z, nx, ny));
+                                else
+                                    store_scaled<S>(dst, ai, m, rho0, sc);
+                            }
                         } else if (exp) {
                             // non-bulk node: hand its pulled populations to the node-list kernel
                             float fw[27];

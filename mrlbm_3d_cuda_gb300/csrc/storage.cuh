@@ -55,6 +55,23 @@ __device__ __forceinline__ Mom decode(const float v[10], float rho0, const Stora
     return m;
 }
 
+// Populations of a node from its raw stored values: FP32 through the moments; 16-bit storage
+// with the storage scales folded into the Hermite factors, so u and m are never unscaled.
+template <typename S>
+__device__ __forceinline__ void rebuild(const float v[10], float rho0, const StorageScale &sc, float f[27]) {
+    if constexpr (std::is_same<S, float>::value) {
+        reconstruct(decode<S>(v, rho0, sc), f);
+    } else {
+        Mom m;
+        m.rho = __fmaf_rn(v[0], sc.is[0], rho0);
+        m.ux = v[1]; m.uy = v[2]; m.uz = v[3];
+        m.mxx = v[4]; m.myy = v[5]; m.mzz = v[6];
+        m.mxy = v[7]; m.mxz = v[8]; m.myz = v[9];
+        reconstruct_h(m, __fmul_rn(3.0f, sc.is[1]), __fmul_rn(1.5f, sc.is[2]), __fmul_rn(4.5f, sc.is[2]),
+                      __fmul_rn(9.0f, sc.is[2]), f);
+    }
+}
+
 // Two 16-bit values of one 32-bit word (lower address first) <-> two floats.
 template <typename S>
 __device__ __forceinline__ float2 pair_to_f(uint32_t w);
@@ -187,6 +204,31 @@ __device__ __forceinline__ void store_mom_sr(S *__restrict__ base, int64_t ai, c
         w[3 * kXBlock] = pair_from_f_sr<S>(m.mzz * sc.s[2], m.mxy * sc.s[2], mix32(key + 0xdaa66d2bu));
         w[4 * kXBlock] = pair_from_f_sr<S>(m.mxz * sc.s[2], m.myz * sc.s[2], mix32(key + 0x78dde6e4u));
     }
+}
+
+// Stores of moments already held with the storage scales (u s_u, m s_m; rho as the full
+// density), as the bulk emit of the step kernel computes them for 16-bit storage.
+template <typename S>
+__device__ __forceinline__ void store_scaled(S *__restrict__ base, int64_t ai, const Mom &m, float rho0,
+                                             const StorageScale &sc) {
+    static_assert(!std::is_same<S, float>::value, "FP32 storage holds physical moments");
+    uint32_t *w = reinterpret_cast<uint32_t *>(base + ai);
+    w[0 * kXBlock] = pair_from_f<S>((m.rho - rho0) * sc.s[0], m.ux);
+    w[1 * kXBlock] = pair_from_f<S>(m.uy, m.uz);
+    w[2 * kXBlock] = pair_from_f<S>(m.mxx, m.myy);
+    w[3 * kXBlock] = pair_from_f<S>(m.mzz, m.mxy);
+    w[4 * kXBlock] = pair_from_f<S>(m.mxz, m.myz);
+}
+template <typename S>
+__device__ __forceinline__ void store_scaled_sr(S *__restrict__ base, int64_t ai, const Mom &m, float rho0,
+                                                const StorageScale &sc, uint32_t key) {
+    static_assert(!std::is_same<S, float>::value, "FP32 storage holds physical moments");
+    uint32_t *w = reinterpret_cast<uint32_t *>(base + ai);
+    w[0 * kXBlock] = pair_from_f_sr<S>((m.rho - rho0) * sc.s[0], m.ux, mix32(key));
+    w[1 * kXBlock] = pair_from_f_sr<S>(m.uy, m.uz, mix32(key + 0x9e3779b9u));
+    w[2 * kXBlock] = pair_from_f_sr<S>(m.mxx, m.myy, mix32(key + 0x3c6ef372u));
+    w[3 * kXBlock] = pair_from_f_sr<S>(m.mzz, m.mxy, mix32(key + 0xdaa66d2bu));
+    w[4 * kXBlock] = pair_from_f_sr<S>(m.mxz, m.myz, mix32(key + 0x78dde6e4u));
 }
 
 }  // namespace mrlbm
