@@ -370,6 +370,48 @@ def run_c5(args):
         print(json.dumps(line), flush=True)
 
 
+# Storage-precision errors measured on a GB300 against the FP64 oracle
+# (tests/test_storage_precision.py): C1 cylinder mean Cd, and max |E / E64 - 1| of the 64^3
+# Taylor-Green vortex over 1000 steps.
+STATED_ERRORS = {"f32": {"c1_cd_rel_err": 1.0e-5, "tgv64_energy_rel_err": 1.0e-6},
+                 "f16": {"c1_cd_rel_err": 5.7e-4, "tgv64_energy_rel_err": 6.9e-4},
+                 "f16_sr": {"c1_cd_rel_err": 2e-7, "tgv64_energy_rel_err": 2.9e-5}}
+
+
+def storage_comparison(args, stream, n, world):
+    """The same Taylor-Green step with FP16 storage, rounding to nearest and stochastically:
+    device-resident MLUPS over min(steps, 1000) timed steps, beside the stated errors."""
+    import torch
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    out = {}
+    k = max(1, min(args.steps, 1000))
+    for name, sr in (("f16", 0), ("f16_sr", 1)):
+        desc = cases.c2_taylor_green(n, STORAGE["f16"])
+        desc.stochastic_rounding = sr
+        sim = Simulation(desc, init=False)
+        sim.set_stream(stream.cuda_stream)
+        sim.init(N.INIT_TAYLOR_GREEN, cases.tgv_params(desc))
+        sim.step(max(3, args.warmup))
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        sim.step(k)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = reduce_max([ev0.elapsed_time(ev1)])[0]
+        nodes = desc.nx * desc.ny * desc.nz
+        value = replica_value(nodes, k, ms * 1e-3, world)
+        peak, _ = measured_peaks()
+        out[name] = {"value": value, "unit": "MLUPS", "steps": k,
+                     "frac_vs_min_traffic": nodes * B_MIN["f16"] / (ms / k * 1e-3) / 1e9 / peak,
+                     **STATED_ERRORS[name]}
+        sim.close()
+    out["f32"] = dict(STATED_ERRORS["f32"])
+    out["errors_from"] = "tests/test_storage_precision.py: GB300 runs against the FP64 oracle"
+    return out
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_info()
@@ -469,6 +511,9 @@ def run_ours(args):
         "gpu_launches": args.steps * ((4 if cyl else 1) + sr),
         "clocks": clk.summary(),
     }
+    if not cyl and storage == "f32" and not args.no_storage_comparison:
+        line["storage_comparison"] = storage_comparison(args, stream, args.n, world)
+        line["storage_comparison"]["f32"]["value"] = value
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(min(args.n, 128), 8, args.cpu_steps, bits=64)
     sim.close()
@@ -498,6 +543,8 @@ def main():
     ap.add_argument("--ref-slab", type=int, default=8)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-storage-comparison", action="store_true",
+                    help="skip the FP16 runs that the default FP32 Taylor-Green line reports beside it")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
