@@ -80,3 +80,29 @@ def test_host_only_handle_refuses_device_calls(built):
     with pytest.raises(N.MrlbmError):
         s.moments()
     s.close()
+
+
+def test_header_and_library_usable_from_plain_c(built, tmp_path):
+    """include/mrlbm.h compiles as C99 with warnings as errors, a C program links against the
+    library and drives it: the shipped cylinder case on the host (2112 wall nodes, 768 BCFLUID
+    nodes, the counts of the reference's own classification) and a status instead of an exit
+    for device work on a host-only handle."""
+    import shutil
+    import subprocess
+    from mrlbm_3d_cuda_gb300 import native as N
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    exe = tmp_path / "abi_from_c"
+    lib_dir = N.LIB_PATH.parent
+    cmd = [cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
+           str(ROOT / "tests" / "c" / "abi_from_c.c"), "-L", str(lib_dir), "-lmrlbm",
+           f"-Wl,-rpath,{lib_dir}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    nx, ny, nz, nb, nbf, rc, note = r.stdout.split()
+    assert (int(nx), int(ny), int(nz)) == (336, 144, 48)
+    assert (int(nb), int(nbf)) == (2112, 768)
+    assert int(rc) == N.ERR_STATE and note == "error-reported"
