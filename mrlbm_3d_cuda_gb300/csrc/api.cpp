@@ -294,9 +294,14 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
             ++h->force_count;
         }
         if (ds) L.diag_part = h->d_diag_part;
+        const int n_step_parts = h->n_ctas + h->n_ctas_sp;
+        // The boundary work of the step runs on the side stream, concurrently with the bulk
+        // tiles: the boundary-tile step kernel, then the node-list kernel (it reads only the
+        // populations that kernel exported) and the wall kernel (it reads only the list
+        // kernel's stencil snapshots); their blocks fill the SMs the bulk launch leaves idle
+        // in its last wave.  No bulk-tile node is read or written by them.
+        cudaStream_t bs = h->stream;
         if (h->n_items_sp > 0) {
-            // boundary tiles on the side stream, concurrently with the bulk tiles: their CTAs
-            // fill the SMs the bulk launch leaves idle in its last wave
             StepLaunch Ls = L;
             Ls.ga = h->d_args_sp;
             Ls.n_ctas = h->n_ctas_sp;
@@ -304,15 +309,15 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
             CK(h, cudaEventRecord(h->ev_fork, h->stream));
             CK(h, cudaStreamWaitEvent(h->side_stream, h->ev_fork, 0));
             CK(h, launch_step(Ls, h->storage, h->tile_y, true, h->side_stream));
-            CK(h, cudaEventRecord(h->ev_join, h->side_stream));
+            bs = h->side_stream;
         }
-        if (h->n_items > 0) CK(h, launch_step(L, h->storage, h->tile_y, false, h->stream));
-        if (h->n_items_sp > 0) CK(h, cudaStreamWaitEvent(h->stream, h->ev_join, 0));
-        const int n_step_parts = h->n_ctas + h->n_ctas_sp;
         if (h->n_list > 0)
             CK(h, launch_special_list(L, h->storage, h->n_list_blocks, ds ? h->d_diag_part + 2 * n_step_parts : nullptr,
-                                      h->stream));
-        if (nb > 0) CK(h, launch_wall(L, h->storage, nb + (fs ? nbf : 0), h->stream));
+                                      bs));
+        if (nb > 0) CK(h, launch_wall(L, h->storage, nb + (fs ? nbf : 0), bs));
+        if (h->n_items_sp > 0) CK(h, cudaEventRecord(h->ev_join, h->side_stream));
+        if (h->n_items > 0) CK(h, launch_step(L, h->storage, h->tile_y, false, h->stream));
+        if (h->n_items_sp > 0) CK(h, cudaStreamWaitEvent(h->stream, h->ev_join, 0));
         if (h->ps_start >= 0 && it >= h->ps_start && it <= h->ps_end) {
             // statistics window: the post-step state (buffer parity ^ 1), as the reference's
             // post_process_step samples it
