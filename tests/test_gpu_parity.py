@@ -173,6 +173,24 @@ def test_annulus_two_walls(cuda_device):
         assert_forces(res, w, comps=(4,))
 
 
+@pytest.mark.parametrize("wall,bcf", [(1, 0), (0, 1), (1, 1)])
+def test_strong_mass_conservation_variants(cuda_device, wall, bcf):
+    """MassBC::Strong for the curved wall (numerical_solution.cu:124-279) and / or for the
+    BCFLUID nodes (the Strong quadratic of boundaries.cuh:890-897 and its mirror images),
+    against the oracle: strict on a short run, the FP32 rounding criterion on a longer one
+    with forces."""
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    desc = cases.cylinder_channel(64, 40, 12, 10, 24.3, 19.7, 0.05, 60.0)
+    desc.mass_bc = N.MASS_STRONG if wall else N.MASS_EQUILIBRIUM
+    desc.bcf_mass_bc = N.MASS_STRONG if bcf else N.MASS_EQUILIBRIUM
+    res = run_pair(desc, 6, N.INIT_REST, fp64=False)
+    assert_fields(res, 0.05, strict=True)
+    res = run_pair(desc, 40, N.INIT_REST, forces=True)
+    assert_fields(res, 0.05)
+    assert_forces(res, 0, comps=(0, 1, 3))
+
+
 BCSOLID_TAGS = [7, 11, 13, 14, 112, 176, 208, 224]
 
 
