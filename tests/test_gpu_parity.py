@@ -191,6 +191,28 @@ def test_strong_mass_conservation_variants(cuda_device, wall, bcf):
     assert_forces(res, 0, comps=(0, 1, 3))
 
 
+@pytest.mark.parametrize("option", ["staircase_z_walls", "periodic_x_array"])
+def test_geometry_options(cuda_device, option):
+    """Remaining combinations of the reference's compile-time switches: staircase wall nodes
+    with no-slip z faces (X_PERIODIC 0, Z_PERIODIC 0, triangular false), and a cylinder in a
+    box periodic in every axis (X_PERIODIC 1: no inlet or outlet; a periodic array of
+    cylinders in a uniform noisy stream)."""
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    if option == "staircase_z_walls":
+        desc = cases.cylinder_channel(64, 32, 12, 8, 20.0, 15.5, 0.05, 40.0, triangular=False, periodic_z=False)
+        init, params = N.INIT_REST, ()
+    else:
+        desc = cases.cylinder_channel(64, 40, 12, 10, 24.3, 19.7, 0.05, 60.0, periodic_y=True)
+        desc.periodic[0] = 1
+        init, params = N.INIT_NOISY_UNIFORM, (0.03, 0.0, 0.0, 0.2, 9)
+    res = run_pair(desc, 6, init, params, fp64=False)
+    assert_fields(res, 0.05, strict=True)
+    res = run_pair(desc, 40, init, params, forces=True)
+    assert_fields(res, 0.05)
+    assert_forces(res, 0, comps=(0, 1))
+
+
 BCSOLID_TAGS = [7, 11, 13, 14, 112, 176, 208, 224]
 
 
