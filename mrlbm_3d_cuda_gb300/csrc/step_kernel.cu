@@ -65,7 +65,7 @@ constexpr bool need_dir(int q, int rcx, int rcy) {
 // Rebuild the populations of one rim column and store the ones the tile pulls from it
 // (rcx, rcy: the c_x / c_y a population must have to enter the tile from this rim side).
 template <typename S, int RCX, int RCY, int TY>
-__device__ __forceinline__ void rim_store(const float raw[10], float rho0, const StorageScale &sc, float *up,
+__device__ __forceinline__ void rim_store(const Raw<S> &raw, float rho0, const StorageScale &sc, float *up,
                                           float *fl, float *dn, int col) {
     constexpr int NC = Geo<TY>::NCOL;
     float f[27];
@@ -164,7 +164,7 @@ __device__ __forceinline__ void gather_all(const float *up, const float *fl, con
 
 // Rebuild the own-column populations of plane p from raw stored moments into the rings.
 template <typename S, int TY>
-__device__ __forceinline__ void arrive_own(const float raw[10], float rho0, const StorageScale &sc, float *up,
+__device__ __forceinline__ void arrive_own(const Raw<S> &raw, float rho0, const StorageScale &sc, float *up,
                                            float *fl, float *dn, int col, float &c0, float &c5, float &c6) {
     float f[27];
     rebuild<S>(raw, rho0, sc, f);
@@ -180,7 +180,7 @@ __device__ __forceinline__ void arrive_own(const float raw[10], float rho0, cons
 }
 
 template <typename S, int TY>
-__device__ __forceinline__ void arrive_rim(const float raw[10], float rho0, const StorageScale &sc, int side, float *up,
+__device__ __forceinline__ void arrive_rim(const Raw<S> &raw, float rho0, const StorageScale &sc, int side, float *up,
                                            float *fl, float *dn, int rcol) {
     switch (side) {
         case 0: rim_store<S, 0, 1, TY>(raw, rho0, sc, up, fl, dn, rcol); break;
@@ -331,9 +331,9 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
 
         // raw moments of planes k (being rebuilt) and k+1 (in flight); the two buffers swap
         // roles every plane, so the plane loops are unrolled by two
-        float pa[10], pb[10];
+        Raw<S> pa, pb;
         const int zm = zs == 0 ? nz - 1 : zs - 1;
-        if (active) load_raw<S>(src, cxy + (int64_t)zm * zst, pa);
+        if (active) load_words<S>(src, cxy + (int64_t)zm * zst, pa);
         int zn = zs;  // plane of the next prefetch (wrapped)
         int k3 = 0, k4 = 0;  // k % 3, k % 4
 
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
             uint32_t wqa = 0u, wqb = 0u;
             int rqa = 0, rqb = 0;
             const unsigned row_mask = w >= 32 ? 0xffffffffu : ((1u << w) - 1u);
-            auto owner_plane = [&](const int k, const float (&cur)[10], float (&nxt)[10], uint32_t &wq, int &rq) {
+            auto owner_plane = [&](const int k, const Raw<S> &cur, Raw<S> &nxt, uint32_t &wq, int &rq) {
                 float *up = up_base + k4 * G::PLANE;
                 float *flt = fl_base + k3 * G::PLANE;
                 float *dn = dn_base + (k & 1) * G::PLANE;
@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 }
                 if (own) {
                     if (k < last) {
-                        load_raw<S>(src, cxy + (int64_t)zn * zst, nxt);
+                        load_words<S>(src, cxy + (int64_t)zn * zst, nxt);
                         zn = zn + 1 == nz ? 0 : zn + 1;
                     }
                     arrive_own<S, TY>(cur, rho0, sc, up, flt, dn, col, c0, c5, c6);
@@ -435,11 +435,11 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 deD += (double)de;
             }
         } else {
-            auto rim_plane = [&](const int k, const float (&cur)[10], float (&nxt)[10]) {
+            auto rim_plane = [&](const int k, const Raw<S> &cur, Raw<S> &nxt) {
                 if (k >= 4) nb_sync(3 + (k & 1), G::NTH);  // DONE(k-2): ring slots of plane k are free
                 if (active) {
                     if (k < last) {
-                        load_raw<S>(src, cxy + (int64_t)zn * zst, nxt);
+                        load_words<S>(src, cxy + (int64_t)zn * zst, nxt);
                         zn = zn + 1 == nz ? 0 : zn + 1;
                     }
                     arrive_rim<S, TY>(cur, rho0, sc, rside, up_base + k4 * G::PLANE, fl_base + k3 * G::PLANE,

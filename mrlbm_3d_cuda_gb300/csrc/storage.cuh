@@ -55,6 +55,23 @@ __device__ __forceinline__ Mom decode(const float v[10], float rho0, const Stora
     return m;
 }
 
+// Stored words of one node as loaded, decoded only where they are used: ten floats for FP32,
+// five 32-bit words (the field pairs) for 16-bit storage.  Prefetching these instead of decoded
+// floats keeps the 16-bit prefetch in flight (a conversion right after the load would wait
+// for it) and in half the registers.
+template <typename S>
+struct Raw {
+    float v[10];
+};
+template <>
+struct Raw<__half> {
+    uint32_t w[5];
+};
+template <>
+struct Raw<__nv_bfloat16> {
+    uint32_t w[5];
+};
+
 // Populations of a node from its raw stored values: FP32 through the moments; 16-bit storage
 // with the storage scales folded into the Hermite factors, so u and m are never unscaled.
 template <typename S>
@@ -154,6 +171,37 @@ __device__ __forceinline__ void load_raw(const S *__restrict__ base, int64_t ai,
             v[2 * j] = f.x;
             v[2 * j + 1] = f.y;
         }
+    }
+}
+
+// Load the stored words of a node without decoding them.
+template <typename S>
+__device__ __forceinline__ void load_words(const S *__restrict__ base, int64_t ai, Raw<S> &r) {
+    if constexpr (std::is_same<S, float>::value) {
+        const float *p = base + ai;
+#pragma unroll
+        for (int k = 0; k < 10; ++k) r.v[k] = p[k * kXBlock];
+    } else {
+        const uint32_t *p = reinterpret_cast<const uint32_t *>(base + ai);
+#pragma unroll
+        for (int j = 0; j < 5; ++j) r.w[j] = p[j * kXBlock];
+    }
+}
+
+// Populations of a node from its loaded words (rebuild of the decoded values).
+template <typename S>
+__device__ __forceinline__ void rebuild(const Raw<S> &r, float rho0, const StorageScale &sc, float f[27]) {
+    if constexpr (std::is_same<S, float>::value) {
+        rebuild<S>(r.v, rho0, sc, f);
+    } else {
+        float v[10];
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+            const float2 t = pair_to_f<S>(r.w[j]);
+            v[2 * j] = t.x;
+            v[2 * j + 1] = t.y;
+        }
+        rebuild<S>(v, rho0, sc, f);
     }
 }
 
