@@ -120,7 +120,8 @@ typedef struct mrlbm_case_desc {
     float wall_u[2][3];   /* UXP/UYP/UZP_INNER and _OUTER: wall velocity in the frame
                              rotated to the local normal (curvedLBM.cu:93-101)            */
     int32_t scan_box[4];  /* x0, x1, y0, y1: window of the node classification scans
-                             (nodeClass.cuh:174-177: LW-4 .. LW+D+4, LS-4 .. LS+D+4)      */
+                             (nodeClass.cuh:174-177: LW-4 .. LW+D+4, LS-4 .. LS+D+4);
+                             all 0: mrlbm_case_desc_finalize derives it from xc, yc, d_wall */
     int32_t triangular;   /* 1: triangular (BCFLUID) classification, 0: staircase         */
     int32_t mass_bc;      /* MASS_CONSERV for the curved wall: MRLBM_MASS_*              */
     int32_t bcf_mass_bc;  /* BCF_MASS_CONSERV for BCFLUID nodes                          */

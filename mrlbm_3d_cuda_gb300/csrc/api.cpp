@@ -481,6 +481,23 @@ int mrlbm_case_desc_finalize(mrlbm_case_desc *d) {
         return fail(nullptr, MRLBM_ERR_INVALID_ARG, "need length > 0 to derive omega");
     if (d->geometry == MRLBM_GEOM_ANNULUS && !(d->d_wall[1] > d->d_wall[0]))
         return fail(nullptr, MRLBM_ERR_INVALID_ARG, "annulus needs d_wall[1] > d_wall[0]");
+    if (d->scan_box[0] == 0 && d->scan_box[1] == 0 && d->scan_box[2] == 0 && d->scan_box[3] == 0) {
+        // classification window left unset: derive it the way the reference's constants do
+        // (nodeClass.cuh:174-177, LW-4 .. LW+D+4 with LW = XC - (D-1)/2; the whole plane for
+        // the annulus, annulus/nodeClass.cuh:311-315), clipped to the grid
+        if (d->geometry == MRLBM_GEOM_CYLINDER) {
+            const int dd = (int)std::ceil(d->d_wall[0]);
+            const int lw = (int)std::floor(d->xc - 0.5f * (d->d_wall[0] - 1.0f));
+            const int ls = (int)std::floor(d->yc - 0.5f * (d->d_wall[0] - 1.0f));
+            d->scan_box[0] = std::max(0, lw - 4);
+            d->scan_box[1] = std::min(d->nx, lw + dd + 4);
+            d->scan_box[2] = std::max(0, ls - 4);
+            d->scan_box[3] = std::min(d->ny, ls + dd + 4);
+        } else {
+            d->scan_box[1] = d->nx;
+            d->scan_box[3] = d->ny;
+        }
+    }
     Derived der;
     const std::string e = derive(*d, der);
     if (!e.empty()) return fail(nullptr, MRLBM_ERR_INVALID_ARG, e);

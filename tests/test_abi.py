@@ -102,7 +102,11 @@ def test_header_and_library_usable_from_plain_c(built, tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
-    nx, ny, nz, nb, nbf, rc, note = r.stdout.split()
+    first, second = r.stdout.splitlines()
+    nx, ny, nz, nb, nbf, rc, note = first.split()
     assert (int(nx), int(ny), int(nz)) == (336, 144, 48)
     assert (int(nb), int(nbf)) == (2112, 768)
     assert int(rc) == N.ERR_STATE and note == "error-reported"
+    # window derived as LW-4 .. LW+D+4 with LW = XC - (D-1)/2 = 24, like cases.cylinder_channel
+    x0, x1, y0, y1, nb2 = (int(v) for v in second.split())
+    assert (x0, x1, y0, y1) == (20, 44, 20, 44) and nb2 > 0
