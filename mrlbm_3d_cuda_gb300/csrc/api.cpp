@@ -213,6 +213,10 @@ int setup_tiling(mrlbm_handle *h, int ty, int lz) {
     h->n_list = (int)list_xyz.size();
     h->n_list_blocks = special_list_blocks(h->n_list);
     const int nseg = (d.nz + h->lz - 1) / h->lz;
+    // work items are int32 `tile | segment << 20` (decoded in step_kernel)
+    if (tiles > (1 << 20) || nseg > (1 << 11))
+        return fail(h, MRLBM_ERR_INVALID_ARG,
+                    "grid too large for the work-item encoding (at most 2^20 xy tiles and 2^11 z segments)");
     // tiles without boundary nodes go to the bulk variant of the step kernel, the others to
     // the variant that reads node words: two launches, each over its own items
     std::vector<int32_t> items, items_sp;
