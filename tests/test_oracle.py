@@ -218,3 +218,44 @@ def test_annulus_couette_profile(built):
     a, b = -om * ri ** 2 / (ro ** 2 - ri ** 2), om * ri ** 2 * ro ** 2 / (ro ** 2 - ri ** 2)
     gap = (r > ri + 2) & (r < ro - 2)
     assert np.abs(ut[gap] - (a * r[gap] + b / r[gap])).max() < 0.015 * ui
+
+
+def test_closed_box_at_rest_is_a_fixed_point(built):
+    """All six faces, twelve edges and eight corners no-slip (no axis periodic, inlet speed
+    0): a fluid at rest stays at rest through every planar closure of boundaries.cuh:201-843
+    (FP64, to round-off)."""
+    import oracle
+    from mrlbm_3d_cuda_gb300 import native as N
+    d = N.default_desc(N.GEOM_NONE)
+    d.nx, d.ny, d.nz = 16, 16, 8
+    d.periodic[0] = d.periodic[1] = d.periodic[2] = 0
+    d.u_max, d.re, d.length, d.omega = 0.0, 10.0, 15.0, 1.2
+    d = N.finalize(d)
+    o = oracle.Oracle(d, 64)
+    assert len(np.unique(o.node_types() >> 20)) == 27  # bulk + 26 boundary classes
+    o.init(N.INIT_REST)
+    o.step(50)
+    assert np.abs(o.moments()).max() < 1e-14
+    o.close()
+
+
+@pytest.mark.parametrize("convective", [0, 1])
+def test_uniform_stream_through_inlet_and_outlet(built, convective):
+    """Velocity inlet (WEST) and zero-gradient or convective outlet (EAST), periodic y and z:
+    the uniform stream u = (U, 0, 0) with m = u u is kept to 1e-8 (its FP64 drift in 50
+    steps is 1.3e-9 in rho - rho0 and 7e-10 in u)."""
+    import oracle
+    from mrlbm_3d_cuda_gb300 import native as N
+    d = N.default_desc(N.GEOM_NONE)
+    d.nx, d.ny, d.nz = 32, 16, 8
+    d.periodic[0], d.periodic[1], d.periodic[2] = 0, 1, 1
+    d.u_max, d.re, d.length = 0.05, 10.0, 15.0
+    d.convective_outlet = convective
+    d = N.finalize(d)
+    o = oracle.Oracle(d, 64)
+    o.init(N.INIT_UNIFORM, (0.05, 0.0, 0.0))
+    o.step(50)
+    m = o.moments()
+    o.close()
+    assert np.abs(m[0]).max() < 1e-8 and np.abs(m[1] - 0.05).max() < 1e-8
+    assert np.abs(m[2:4]).max() < 1e-14 and np.abs(m[4] - 0.05 ** 2).max() < 1e-8
