@@ -5,6 +5,12 @@ sources, where they lie, into oracle/_ref/ — test infrastructure only.
   classification for its shipped cylinder case and dumps the result (see
   ref_harness/ref_geometry.cu).  Built when the reference tree is present (this
   container); the GPU machine has no reference tree and uses nothing from here.
+* ``ref_geometry_annulus``: the annulus case's classification for both walls
+  (ref_harness/ref_geometry_annulus.cu).  The reference selects the case at compile time
+  (``#define CASE_ID`` in config.h:8), and its annulus case does not compile as shipped:
+  statistics/stat_header.cuh reads ``h_rho_inlet`` / ``h_rho_inlet_average``, which only the
+  cylinder's constants define.  The staged copy sets CASE_ID to CASE_ANNULUS and adds those
+  two host globals to cases/annulus/constants.cuh; nothing else changes.
 * ``ref_geometry_zwall``: the same harness for the shipped case with z walls.  The reference
   selects that at compile time (``#define Z_PERIODIC`` in cases/cylinder/constants.cuh:10),
   so its src/ tree is copied to a temporary directory, that one line is set to 0, the
@@ -82,8 +88,48 @@ def build_ref_geometry_zwall(force: bool = False) -> Path | None:
     return exe
 
 
+def _staged_build(name: str, harness: str, edits, force: bool) -> Path | None:
+    """Compile `harness` against a temporary copy of the reference's src/ with `edits`
+    (relative path, old line start, new line or None to append) applied."""
+    if not reference_present():
+        return None
+    exe = OUT / name
+    src = HERE / "ref_harness" / harness
+    if not force and exe.exists() and exe.stat().st_mtime > src.stat().st_mtime:
+        return exe
+    OUT.mkdir(exist_ok=True)
+    with tempfile.TemporaryDirectory() as td:
+        tree = Path(td) / "src"
+        shutil.copytree(REF_SRC, tree, ignore=shutil.ignore_patterns("*.o"))
+        for rel, old, new in edits:
+            f = tree / rel
+            lines = f.read_text().split("\n")
+            if old is None:
+                lines.append(new)
+            else:
+                hits = [i for i, ln in enumerate(lines) if ln.strip().startswith(old)]
+                if len(hits) != 1:
+                    raise RuntimeError(f"cannot find '{old}' in {rel}")
+                lines[hits[0]] = new
+            f.write_text("\n".join(lines))
+        cmd = [_nvcc(), "-std=c++17", "-O2", "-x", "cu", "-gencode", "arch=compute_103a,code=sm_103a",
+               "-I", str(tree), "-I", str(REF_SRC.parent), '-DID_SIM="000"', "-w", str(src), "-o", str(exe)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference harness {name} failed to build:\n{' '.join(cmd)}\n{r.stderr}")
+    return exe
+
+
+def build_ref_geometry_annulus(force: bool = False) -> Path | None:
+    return _staged_build("ref_geometry_annulus", "ref_geometry_annulus.cu", [
+        ("config.h", "#define CASE_ID CASE_CYLINDER", "#define CASE_ID CASE_ANNULUS"),
+        ("cases/annulus/constants.cuh", None, "inline real h_rho_inlet = 1.0, h_rho_inlet_average = 0.0;"),
+    ], force)
+
+
 def build(force: bool = False) -> dict:
-    return {"ref_geometry": build_ref_geometry(force), "ref_geometry_zwall": build_ref_geometry_zwall(force)}
+    return {"ref_geometry": build_ref_geometry(force), "ref_geometry_zwall": build_ref_geometry_zwall(force),
+            "ref_geometry_annulus": build_ref_geometry_annulus(force)}
 
 
 if __name__ == "__main__":

@@ -11,6 +11,11 @@ ref_cylinder_zwall_geometry.npz — the same for that case with z walls (Z_PERIO
 oracle/_ref/ref_geometry_zwall): adds the BCSOLID nodes on the z = 0 and z = NZ - 1 faces
 (cases/cylinder/nodeClass.cuh:254-287) and their list.
 
+ref_annulus_geometry.npz — the reference's classification of its shipped annulus case
+(136 x 136 x 256, r 32 / 64) for both walls (oracle/_ref/ref_geometry_annulus): node types of
+the z = 0 and z = 255 planes plus a SHA-256 of the whole array, per-wall lists, normals, wall
+distances and masks, and the per-tag BCFLUID masks.
+
 ref_geometry_files.json — SHA-256 and size of each grid_layout/*.dat file the reference's own
 write_geometry_files (cases/cylinder/cylinder_helpers.cuh:388-470) writes for both builds.
 
@@ -31,7 +36,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
-from oracle.build_ref import build_ref_geometry, build_ref_geometry_zwall  # noqa: E402
+from oracle.build_ref import build_ref_geometry, build_ref_geometry_annulus, build_ref_geometry_zwall  # noqa: E402
 
 
 def tiled_to_lex(idx: np.ndarray, nx: int, ny: int, nz: int) -> np.ndarray:
@@ -76,6 +81,37 @@ def make_geometry(out: Path, zwall: bool = False):
         )
 
 
+def make_annulus(out: Path):
+    exe = build_ref_geometry_annulus()
+    if exe is None:
+        raise SystemExit("reference tree not present: cannot regenerate")
+    with tempfile.TemporaryDirectory() as td:
+        subprocess.run([str(exe), td], check=True, capture_output=True)
+        d = Path(td)
+        rd = lambda name, dt: np.fromfile(d / name, dtype=dt)  # noqa: E731
+        meta = rd("meta.i32", np.int32)
+        nx, ny, nz = (int(v) for v in meta[:3])
+        tiled = rd("node_type_tiled.u32", np.uint32)
+        lex = tiled_to_lex(np.arange(nx * ny * nz), nx, ny, nz)
+        types = np.empty_like(tiled)
+        types[lex] = tiled
+        plane = nx * ny
+        arrays = dict(shape=np.array([nx, ny, nz], dtype=np.int32),
+                      nb=meta[[3, 5]].astype(np.int32), nb_fluid=meta[[4, 6]].astype(np.int32),
+                      types_first_plane=types[:plane], types_last_plane=types[-plane:],
+                      types_sha256=np.frombuffer(hashlib.sha256(types.tobytes()).digest(), dtype=np.uint8),
+                      tag_in_mask=rd("tag_in_mask.u32", np.uint32), tag_out_mask=rd("tag_out_mask.u32", np.uint32))
+        for w in ("inner", "outer"):
+            arrays[f"{w}_boundary_list"] = tiled_to_lex(rd(f"{w}_boundary_list_tiled.u64", np.uint64), nx, ny, nz)
+            arrays[f"{w}_unit_nx"] = rd(f"{w}_unit_nx.f32", np.float32)
+            arrays[f"{w}_unit_ny"] = rd(f"{w}_unit_ny.f32", np.float32)
+            arrays[f"{w}_delta"] = rd(f"{w}_delta_w.f32", np.float32)
+            arrays[f"{w}_in_mask"] = rd(f"{w}_in_mask.u32", np.uint32)
+            arrays[f"{w}_out_mask"] = rd(f"{w}_out_mask.u32", np.uint32)
+            arrays[f"{w}_fluid_list"] = tiled_to_lex(rd(f"{w}_bcfluid_list_tiled.u64", np.uint64), nx, ny, nz)
+        np.savez_compressed(out, **arrays)
+
+
 def make_geometry_files(out: Path):
     res = {}
     for variant, build in (("periodic_z", build_ref_geometry), ("z_walls", build_ref_geometry_zwall)):
@@ -97,3 +133,5 @@ if __name__ == "__main__":
         print("wrote", here / name)
     make_geometry_files(here / "ref_geometry_files.json")
     print("wrote", here / "ref_geometry_files.json")
+    make_annulus(here / "ref_annulus_geometry.npz")
+    print("wrote", here / "ref_annulus_geometry.npz")
