@@ -36,10 +36,13 @@ def reference_cylinder(storage: int = N.STORAGE_F32, diameter: int = 16, *, peri
     return _finish(d, storage)
 
 
-def reference_annulus(storage: int = N.STORAGE_F32) -> N.CaseDesc:
+def reference_annulus(storage: int = N.STORAGE_F32, *, periodic_z: bool = True) -> N.CaseDesc:
     """The reference's shipped annulus case (cases/annulus/constants.cuh:8-84):
-    136 x 136 x 256, r = 32 / 64 about (67.5, 67.5), inner wall speed 0.03, Re = 70."""
-    return _finish(N.default_desc(N.GEOM_ANNULUS), storage)
+    136 x 136 x 256, r = 32 / 64 about (67.5, 67.5), inner wall speed 0.03, Re = 70.
+    `periodic_z=False` is that case with Z_PERIODIC 0 (constants.cuh:10)."""
+    d = N.default_desc(N.GEOM_ANNULUS)
+    d.periodic[2] = int(periodic_z)
+    return _finish(d, storage)
 
 
 def cylinder_channel(nx: int, ny: int, nz: int, d: float, xc: float, yc: float, u: float, re: float, *,

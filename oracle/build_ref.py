@@ -11,6 +11,8 @@ sources, where they lie, into oracle/_ref/ — test infrastructure only.
   statistics/stat_header.cuh reads ``h_rho_inlet`` / ``h_rho_inlet_average``, which only the
   cylinder's constants define.  The staged copy sets CASE_ID to CASE_ANNULUS and adds those
   two host globals to cases/annulus/constants.cuh; nothing else changes.
+* ``ref_geometry_annulus_zwall``: the same with ``#define Z_PERIODIC 0`` in the annulus
+  constants (BCSOLID nodes on both walls).
 * ``ref_geometry_zwall``: the same harness for the shipped case with z walls.  The reference
   selects that at compile time (``#define Z_PERIODIC`` in cases/cylinder/constants.cuh:10),
   so its src/ tree is copied to a temporary directory, that one line is set to 0, the
@@ -127,9 +129,18 @@ def build_ref_geometry_annulus(force: bool = False) -> Path | None:
     ], force)
 
 
+def build_ref_geometry_annulus_zwall(force: bool = False) -> Path | None:
+    return _staged_build("ref_geometry_annulus_zwall", "ref_geometry_annulus.cu", [
+        ("config.h", "#define CASE_ID CASE_CYLINDER", "#define CASE_ID CASE_ANNULUS"),
+        ("cases/annulus/constants.cuh", None, "inline real h_rho_inlet = 1.0, h_rho_inlet_average = 0.0;"),
+        ("cases/annulus/constants.cuh", "#define Z_PERIODIC 1", "#define Z_PERIODIC 0"),
+    ], force)
+
+
 def build(force: bool = False) -> dict:
     return {"ref_geometry": build_ref_geometry(force), "ref_geometry_zwall": build_ref_geometry_zwall(force),
-            "ref_geometry_annulus": build_ref_geometry_annulus(force)}
+            "ref_geometry_annulus": build_ref_geometry_annulus(force),
+            "ref_geometry_annulus_zwall": build_ref_geometry_annulus_zwall(force)}
 
 
 if __name__ == "__main__":

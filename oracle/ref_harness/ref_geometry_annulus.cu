@@ -1,7 +1,7 @@
 // Geometry pin for the annulus: drives the reference's own host-side node classification
 // (sakthi-lbm/MRLBM_3D_CUDA, shipped annulus case, compiled with CASE_ID = CASE_ANNULUS) and
-// dumps it for both walls, so the oracle's and the product's restatements can be checked
-// against it.  Test infrastructure only; no GPU is used: the calls follow
+// dumps it for both walls (and the BCSOLID lists of a Z_PERIODIC 0 build), so the oracle's
+// and the product's restatements can be checked against it.  Test infrastructure only; no GPU is used: the calls follow
 // cases/annulus/annulus_kernels.cu:5-49 (annulus_initialize) on malloc'd arrays.
 #include <cstdio>
 #include <cstdlib>
@@ -43,6 +43,7 @@ static void dump_wall(const std::string &out, const char *tag, const boundaryVar
     dump(out, name("in_mask.u32").c_str(), b.incomingMask, b.NB * sizeof(uint32_t));
     dump(out, name("out_mask.u32").c_str(), b.outgoingMask, b.NB * sizeof(uint32_t));
     dump(out, name("bcfluid_list_tiled.u64").c_str(), b.bcfluidList, b.NB_FLUID * sizeof(size_t));
+    dump(out, name("bcsolid_list_tiled.u64").c_str(), b.bcsolidList, b.NB_SOLID * sizeof(size_t));
 }
 
 int main(int argc, char **argv) {
@@ -69,7 +70,8 @@ int main(int argc, char **argv) {
     setup_bcfluid_masks(h, in);
     setup_bcfluid_masks(h, outer);
 
-    const int meta[8] = {NX, NY, NZ, in.NB, in.NB_FLUID, outer.NB, outer.NB_FLUID, 0};
+    const int meta[10] = {NX, NY, NZ, in.NB, in.NB_FLUID, outer.NB, outer.NB_FLUID, in.NB_SOLID, outer.NB_SOLID,
+                          Z_PERIODIC};
     dump(out, "meta.i32", meta, sizeof(meta));
     dump(out, "node_type_tiled.u32", h.nodeType, NUM_LBM_NODES * sizeof(nodeType_t));
     dump_wall(out, "inner", in);

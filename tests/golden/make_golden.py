@@ -14,7 +14,8 @@ oracle/_ref/ref_geometry_zwall): adds the BCSOLID nodes on the z = 0 and z = NZ 
 ref_annulus_geometry.npz — the reference's classification of its shipped annulus case
 (136 x 136 x 256, r 32 / 64) for both walls (oracle/_ref/ref_geometry_annulus): node types of
 the z = 0 and z = 255 planes plus a SHA-256 of the whole array, per-wall lists, normals, wall
-distances and masks, and the per-tag BCFLUID masks.
+distances and masks, and the per-tag BCFLUID masks.  ref_annulus_zwall_geometry.npz: the same
+for that case built with Z_PERIODIC 0, with both walls' BCSOLID lists.
 
 ref_geometry_files.json — SHA-256 and size of each grid_layout/*.dat file the reference's own
 write_geometry_files (cases/cylinder/cylinder_helpers.cuh:388-470) writes for both builds.
@@ -36,7 +37,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
-from oracle.build_ref import build_ref_geometry, build_ref_geometry_annulus, build_ref_geometry_zwall  # noqa: E402
+from oracle.build_ref import (build_ref_geometry, build_ref_geometry_annulus,  # noqa: E402
+                              build_ref_geometry_annulus_zwall, build_ref_geometry_zwall)
 
 
 def tiled_to_lex(idx: np.ndarray, nx: int, ny: int, nz: int) -> np.ndarray:
@@ -81,8 +83,8 @@ def make_geometry(out: Path, zwall: bool = False):
         )
 
 
-def make_annulus(out: Path):
-    exe = build_ref_geometry_annulus()
+def make_annulus(out: Path, zwall: bool = False):
+    exe = build_ref_geometry_annulus_zwall() if zwall else build_ref_geometry_annulus()
     if exe is None:
         raise SystemExit("reference tree not present: cannot regenerate")
     with tempfile.TemporaryDirectory() as td:
@@ -98,6 +100,7 @@ def make_annulus(out: Path):
         plane = nx * ny
         arrays = dict(shape=np.array([nx, ny, nz], dtype=np.int32),
                       nb=meta[[3, 5]].astype(np.int32), nb_fluid=meta[[4, 6]].astype(np.int32),
+                      nb_solid=meta[[7, 8]].astype(np.int32), z_periodic=np.int32(meta[9]),
                       types_first_plane=types[:plane], types_last_plane=types[-plane:],
                       types_sha256=np.frombuffer(hashlib.sha256(types.tobytes()).digest(), dtype=np.uint8),
                       tag_in_mask=rd("tag_in_mask.u32", np.uint32), tag_out_mask=rd("tag_out_mask.u32", np.uint32))
@@ -109,6 +112,7 @@ def make_annulus(out: Path):
             arrays[f"{w}_in_mask"] = rd(f"{w}_in_mask.u32", np.uint32)
             arrays[f"{w}_out_mask"] = rd(f"{w}_out_mask.u32", np.uint32)
             arrays[f"{w}_fluid_list"] = tiled_to_lex(rd(f"{w}_bcfluid_list_tiled.u64", np.uint64), nx, ny, nz)
+            arrays[f"{w}_solid_list"] = tiled_to_lex(rd(f"{w}_bcsolid_list_tiled.u64", np.uint64), nx, ny, nz)
         np.savez_compressed(out, **arrays)
 
 
@@ -133,5 +137,6 @@ if __name__ == "__main__":
         print("wrote", here / name)
     make_geometry_files(here / "ref_geometry_files.json")
     print("wrote", here / "ref_geometry_files.json")
-    make_annulus(here / "ref_annulus_geometry.npz")
-    print("wrote", here / "ref_annulus_geometry.npz")
+    for name, zwall in (("ref_annulus_geometry.npz", False), ("ref_annulus_zwall_geometry.npz", True)):
+        make_annulus(here / name, zwall)
+        print("wrote", here / name)

@@ -142,17 +142,19 @@ def test_geometry_files_match_reference_writer(built, tmp_path, variant):
         assert want["bcsolid_inner.dat"]["bytes"] > 0
 
 
-def test_product_and_oracle_annulus_geometry_match_reference(built):
-    """The shipped annulus case (136 x 136 x 256, r 32 / 64) against the reference's own
-    classification of both walls (oracle/_ref/ref_geometry_annulus, fixture made by
-    tests/golden/make_golden.py): every node type (SHA-256 of the whole array plus the end
-    planes in full), each wall's list, normals, wall distances and masks, and the per-tag
-    BCFLUID masks (the outer wall's pass writes last, as in annulus_kernels.cu:37-38)."""
+@pytest.mark.parametrize("fixture", ["ref_annulus_geometry.npz", "ref_annulus_zwall_geometry.npz"])
+def test_product_and_oracle_annulus_geometry_match_reference(built, fixture):
+    """The shipped annulus case (136 x 136 x 256, r 32 / 64), periodic in z and with z walls,
+    against the reference's own classification of both walls (oracle/_ref/ref_geometry_annulus*,
+    fixtures made by tests/golden/make_golden.py): every node type (SHA-256 of the whole array
+    plus the end planes in full), each wall's list, normals, wall distances, masks and BCSOLID
+    list, and the per-tag BCFLUID masks (the outer wall's pass writes last, as in
+    annulus_kernels.cu:37-38)."""
     import hashlib
     import oracle
     from mrlbm_3d_cuda_gb300 import Simulation, cases
-    g = np.load(GOLDEN / "ref_annulus_geometry.npz")
-    desc = cases.reference_annulus()
+    g = np.load(GOLDEN / fixture)
+    desc = cases.reference_annulus(periodic_z=bool(int(g["z_periodic"])))
     plane = desc.nx * desc.ny
     s = Simulation(desc, host_only=True)
     o = oracle.Oracle(desc, 64)
@@ -163,9 +165,11 @@ def test_product_and_oracle_annulus_geometry_match_reference(built):
         assert hashlib.sha256(types.astype(np.uint32).tobytes()).digest() == g["types_sha256"].tobytes()
         for w, b in (("inner", b0), ("outer", b1)):
             for k, gk in (("list", "boundary_list"), ("nx", "unit_nx"), ("ny", "unit_ny"), ("delta", "delta"),
-                          ("in_mask", "in_mask"), ("out_mask", "out_mask"), ("fluid_list", "fluid_list")):
+                          ("in_mask", "in_mask"), ("out_mask", "out_mask"), ("fluid_list", "fluid_list"),
+                          ("solid_list", "solid_list")):
                 assert np.array_equal(b[k], g[f"{w}_{gk}"]), (w, k)
         assert np.array_equal(b0["tag_in_mask"], g["tag_in_mask"])
         assert np.array_equal(b0["tag_out_mask"], g["tag_out_mask"])
     assert list(g["nb"]) == [s.info.nb[0], s.info.nb[1]]
+    assert list(g["nb_solid"]) == [s.info.nb_solid[0], s.info.nb_solid[1]]
     o.close()
