@@ -11,6 +11,8 @@ sources, where they lie, into oracle/_ref/ — test infrastructure only.
   statistics/stat_header.cuh reads ``h_rho_inlet`` / ``h_rho_inlet_average``, which only the
   cylinder's constants define.  The staged copy sets CASE_ID to CASE_ANNULUS and adds those
   two host globals to cases/annulus/constants.cuh; nothing else changes.
+* ``ref_geometry_staircase``: the cylinder harness with ``triangular = false``
+  (cases/cylinder/constants.cuh:15): the staircase classification.
 * ``ref_geometry_annulus_zwall``: the same with ``#define Z_PERIODIC 0`` in the annulus
   constants (BCSOLID nodes on both walls).
 * ``ref_geometry_zwall``: the same harness for the shipped case with z walls.  The reference
@@ -137,8 +139,15 @@ def build_ref_geometry_annulus_zwall(force: bool = False) -> Path | None:
     ], force)
 
 
+def build_ref_geometry_staircase(force: bool = False) -> Path | None:
+    return _staged_build("ref_geometry_staircase", "ref_geometry.cu", [
+        ("cases/cylinder/constants.cuh", "constexpr bool triangular = true;", "constexpr bool triangular = false;"),
+    ], force)
+
+
 def build(force: bool = False) -> dict:
     return {"ref_geometry": build_ref_geometry(force), "ref_geometry_zwall": build_ref_geometry_zwall(force),
+            "ref_geometry_staircase": build_ref_geometry_staircase(force),
             "ref_geometry_annulus": build_ref_geometry_annulus(force),
             "ref_geometry_annulus_zwall": build_ref_geometry_annulus_zwall(force)}
 

@@ -6,7 +6,7 @@
 // Compiled by oracle/build_ref.py from the reference sources where they lie
 // (-I <reference>/MRLBM_3D/src); nothing here runs on a GPU: only inline host functions of
 //   solver/initializeLBM.cuh:58-80 (initialize_nodeType -> boundary_definitions),
-//   cases/cylinder/nodeClass.cuh:299-324 (initialize_cylinder_nodeType_triangular),
+//   cases/cylinder/nodeClass.cuh:289-324 (initialize_cylinder_nodeType_triangular / _staircase),
 //   cases/cylinder/cylinder_helpers.cuh:10-299 (lists, indices, normals, masks)
 // are called, on malloc'd arrays in place of the cudaMallocHost ones of
 // cylinder_kernels.cuh:406-465.
@@ -42,7 +42,8 @@ int main(int argc, char **argv) {
     h.nodeType = (nodeType_t *)calloc(NUM_LBM_NODES, sizeof(nodeType_t));
     initialize_nodeType(h);
     boundaryVar b{};
-    initialize_cylinder_nodeType_triangular(h, b);
+    if (triangular) initialize_cylinder_nodeType_triangular(h, b);
+    else initialize_cylinder_nodeType_staircase(h, b);
     b.boundaryList = (size_t *)malloc(b.NB * sizeof(size_t));
     b.incomingMask = (uint32_t *)malloc(b.NB * sizeof(uint32_t));
     b.outgoingMask = (uint32_t *)malloc(b.NB * sizeof(uint32_t));
@@ -58,8 +59,10 @@ int main(int argc, char **argv) {
     assignBoundaryIndices(h, b, NODE_INNER);
     compute_unit_vectors_boundary_nodes(h, b, D_WALL);
     find_incomings_outgoings(h, b);
-    setup_bcfluid_masks(h, b);
-    setup_bcsolid_masks(h, b);
+    if (triangular) {
+        setup_bcfluid_masks(h, b);
+        setup_bcsolid_masks(h, b);
+    }
 
     const int meta[8] = {NX, NY, NZ, b.NB, b.NB_FLUID, b.NB_SOLID, Z_PERIODIC, 0};
     const float fmeta[4] = {XC, YC, D_WALL, (float)OMEGA};

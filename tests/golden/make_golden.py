@@ -7,6 +7,9 @@ sources by oracle/build_ref.py).  Index arrays are converted from the reference'
 IDX_BLOCK order to lexicographic x + NX (y + NY z); the full node-type array is stored
 lexicographic too.
 
+ref_cylinder_staircase_geometry.npz — the same case with the staircase classification
+(triangular = false, oracle/_ref/ref_geometry_staircase).
+
 ref_cylinder_zwall_geometry.npz — the same for that case with z walls (Z_PERIODIC 0,
 oracle/_ref/ref_geometry_zwall): adds the BCSOLID nodes on the z = 0 and z = NZ - 1 faces
 (cases/cylinder/nodeClass.cuh:254-287) and their list.
@@ -38,7 +41,8 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
 from oracle.build_ref import (build_ref_geometry, build_ref_geometry_annulus,  # noqa: E402
-                              build_ref_geometry_annulus_zwall, build_ref_geometry_zwall)
+                              build_ref_geometry_annulus_zwall, build_ref_geometry_staircase,
+                              build_ref_geometry_zwall)
 
 
 def tiled_to_lex(idx: np.ndarray, nx: int, ny: int, nz: int) -> np.ndarray:
@@ -52,8 +56,8 @@ def tiled_to_lex(idx: np.ndarray, nx: int, ny: int, nz: int) -> np.ndarray:
     return x + nx * (y + ny * z)
 
 
-def make_geometry(out: Path, zwall: bool = False):
-    exe = build_ref_geometry_zwall() if zwall else build_ref_geometry()
+def make_geometry(out: Path, zwall: bool = False, staircase: bool = False):
+    exe = build_ref_geometry_zwall() if zwall else (build_ref_geometry_staircase() if staircase else build_ref_geometry())
     if exe is None:
         raise SystemExit("reference tree not present: cannot regenerate")
     with tempfile.TemporaryDirectory() as td:
@@ -132,8 +136,10 @@ def make_geometry_files(out: Path):
 
 if __name__ == "__main__":
     here = Path(__file__).resolve().parent
-    for name, zwall in (("ref_cylinder_geometry.npz", False), ("ref_cylinder_zwall_geometry.npz", True)):
-        make_geometry(here / name, zwall)
+    for name, zwall, stair in (("ref_cylinder_geometry.npz", False, False),
+                               ("ref_cylinder_zwall_geometry.npz", True, False),
+                               ("ref_cylinder_staircase_geometry.npz", False, True)):
+        make_geometry(here / name, zwall, stair)
         print("wrote", here / name)
     make_geometry_files(here / "ref_geometry_files.json")
     print("wrote", here / "ref_geometry_files.json")

@@ -60,6 +60,25 @@ def test_reference_tiled_layout_round_trip(built, golden):
     assert np.array_equal(back, golden["node_types"])
 
 
+def test_product_and_oracle_staircase_geometry_match_reference(built):
+    """The shipped cylinder case with the staircase classification (triangular = false,
+    cases/cylinder/nodeClass.cuh:138-167, 289-297) against the reference's own host code."""
+    import oracle
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    g = np.load(GOLDEN / "ref_cylinder_staircase_geometry.npz")
+    desc = cases.reference_cylinder()
+    desc.triangular = 0
+    s = Simulation(desc, host_only=True)
+    o = oracle.Oracle(desc, 64)
+    for types, b in ((s.node_types(), s.boundary(0)), (o.node_types(), o.boundary(0))):
+        assert np.array_equal(types, g["node_types"])
+        for k, gk in KEYS[:6]:
+            assert np.array_equal(b[k], g[gk]), k
+        assert len(b["fluid_list"]) == 0
+    assert int(g["nb"]) == 2880 and int(g["nb_fluid"]) == 0
+    o.close()
+
+
 @pytest.fixture(scope="module")
 def golden_zwall():
     return np.load(GOLDEN / "ref_cylinder_zwall_geometry.npz")
