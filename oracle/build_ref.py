@@ -146,10 +146,15 @@ def build_ref_geometry_staircase(force: bool = False) -> Path | None:
 
 
 def build(force: bool = False) -> dict:
-    return {"ref_geometry": build_ref_geometry(force), "ref_geometry_zwall": build_ref_geometry_zwall(force),
-            "ref_geometry_staircase": build_ref_geometry_staircase(force),
-            "ref_geometry_annulus": build_ref_geometry_annulus(force),
-            "ref_geometry_annulus_zwall": build_ref_geometry_annulus_zwall(force)}
+    """Every harness variant, compiled concurrently (one nvcc each)."""
+    from concurrent.futures import ThreadPoolExecutor
+    jobs = {"ref_geometry": build_ref_geometry, "ref_geometry_zwall": build_ref_geometry_zwall,
+            "ref_geometry_staircase": build_ref_geometry_staircase,
+            "ref_geometry_annulus": build_ref_geometry_annulus,
+            "ref_geometry_annulus_zwall": build_ref_geometry_annulus_zwall}
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        futures = {name: ex.submit(fn, force) for name, fn in jobs.items()}
+        return {name: f.result() for name, f in futures.items()}
 
 
 if __name__ == "__main__":
