@@ -9,7 +9,7 @@ ABI with host buffers: the initial moment field is uploaded from pinned memory, 
 reads back its FP64 mass / energy sample, and the final field is read back, all inside the
 timed region.  The reference arm (--impl reference) times the CPU restatement of the
 reference algorithm (the reference has no CPU path) on a bounded slab of the same workload.
-Multi-GPU: the path does not shard across GPUs in this build, so N > 1 runs N independent
+Multi-GPU: no z-slab exchange between GPUs is implemented, so N > 1 runs N independent
 replicas (weak scaling), one per rank.
 """
 from __future__ import annotations
