@@ -62,6 +62,7 @@ class Simulation:
 
     # ---- lifecycle ----------------------------------------------------------------------
     def close(self):
+        """Destroy the handle (mrlbm_destroy) unless a batch owns it."""
         if getattr(self, "_h", None) is not None and self._h.value:
             if getattr(self, "_owned", True):
                 N.lib().mrlbm_destroy(self._h)
@@ -90,25 +91,35 @@ class Simulation:
         return tuple(t)
 
     def get_info(self) -> N.Info:
+        """Sizes, wall counts, omega / tau, step, storage and tiling (mrlbm_get_info)."""
         info = N.Info()
         self._ck(N.lib().mrlbm_get_info(self._h, C.byref(info)))
         return info
 
     def set_stream(self, stream_ptr: int | None):
+        """Launch on the caller's cudaStream_t (a raw handle; None or 0: the handle's own stream)."""
         self._ck(N.lib().mrlbm_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
 
     # ---- time stepping ------------------------------------------------------------------
     def init(self, kind: int = N.INIT_REFERENCE_NOISE, params: Sequence[float] = ()):
+        """Initial field (mrlbm_init): INIT_REFERENCE_NOISE reproduces the reference's initial
+        state bit for bit; TAYLOR_GREEN (u0, L), UNIFORM (ux, uy, uz), NOISY_UNIFORM (ux, uy,
+        uz, amplitude, seed), REST."""
         arr = (C.c_double * max(1, len(params)))(*params)
         self._ck(N.lib().mrlbm_init(self._h, kind, arr, len(params)))
 
     def step(self, n: int = 1):
+        """Advance n time steps, asynchronously on the handle's stream (mrlbm_step)."""
         self._ck(N.lib().mrlbm_step(self._h, int(n)))
 
     def set_sampling(self, force_every: int = 0, diag_every: int = 0):
+        """Record wall forces every force_every steps and FP64 mass / energy every diag_every steps
+        (0: off)."""
         self._ck(N.lib().mrlbm_set_sampling(self._h, int(force_every), int(diag_every)))
 
     def sync(self):
+        """Wait for the queued steps; raises on a device error or non-finite diagnostics
+        (MRLBM_ERR_DIVERGED)."""
         self._ck(N.lib().mrlbm_sync(self._h))
 
     def run(self, max_iter: int, macr_save: int = 0, stat_start: int = 0, stat_end: int = -1):
@@ -135,11 +146,15 @@ class Simulation:
         return out.reshape(nf, self.n)
 
     def set_moments(self, values: np.ndarray, fields="all", layout: int = N.LAYOUT_LEXICOGRAPHIC):
+        """Upload FP32 moments (shape as moments() returns) into both ping-pong buffers, storage-
+        encoded."""
         mask = N.field_mask(fields)
         v = N.as_f32(values)
         self._ck(N.lib().mrlbm_set_moments(self._h, mask, layout, v.ctypes.data_as(C.c_void_p), v.size))
 
     def node_types(self, layout: int = N.LAYOUT_LEXICOGRAPHIC) -> np.ndarray:
+        """Node types in the reference's encoding: class << 20 | wall index or BCFLUID / BCSOLID
+        tag."""
         out = np.empty(self.n, dtype=np.uint32)
         self._ck(N.lib().mrlbm_get_node_types(self._h, layout, out.ctypes.data_as(C.c_void_p), out.size))
         return out
@@ -171,6 +186,7 @@ class Simulation:
         return out.reshape(2, 5)
 
     def force_history(self, max_steps: int = 1 << 16):
+        """(steps, forces) of the sampled steps still in the ring; forces shaped (n, 2 walls, 5)."""
         steps = np.zeros(max_steps, dtype=np.int64)
         f = np.zeros((max_steps, 10), dtype=np.float64)
         n = C.c_int32()
@@ -189,12 +205,15 @@ class Simulation:
 
     # ---- files ------------------------------------------------------------------------------
     def checkpoint_save(self, path: str):
+        """Write restart.bin in the reference's format (step, tiled moments, face populations)."""
         self._ck(N.lib().mrlbm_checkpoint_save(self._h, str(path).encode()))
 
     def checkpoint_load(self, path: str):
+        """Load a restart.bin written by this library or by the reference."""
         self._ck(N.lib().mrlbm_checkpoint_load(self._h, str(path).encode()))
 
     def write_vti(self, path: str):
+        """Write the current field as the reference's raw-appended .vti (rho, ux, uy, uz)."""
         self._ck(N.lib().mrlbm_write_vti(self._h, str(path).encode()))
 
     def write_forces(self, forces_path: str | None, mass_path: str | None = None, wall: int = 0,
@@ -209,6 +228,7 @@ class Simulation:
         self._ck(N.lib().mrlbm_set_pressure_window(self._h, int(start), int(end)))
 
     def write_pressure(self, path: str, wall: int = 0):
+        """pressure.dat (`theta z Cp`) of the statistics window's averaged wall pressure."""
         self._ck(N.lib().mrlbm_write_pressure(self._h, int(wall), str(path).encode()))
 
     def write_inlet_density(self, path: str, append: bool = False):
@@ -283,6 +303,7 @@ class Batch:
         return len(self.cases)
 
     def close(self):
+        """Destroy the batch and its cases (mrlbm_batch_destroy)."""
         if getattr(self, "_b", None) is not None and self._b.value:
             for c in self.cases:
                 c.close()
@@ -296,15 +317,19 @@ class Batch:
             pass
 
     def set_sampling(self, force_every: int):
+        """Record every case's wall forces every force_every steps (0: off)."""
         N.check(N.lib().mrlbm_batch_set_sampling(self._b, int(force_every)))
 
     def step(self, n: int = 1):
+        """Advance every case n steps with the batched, graph-replayed launches."""
         N.check(N.lib().mrlbm_batch_step(self._b, int(n)))
 
     def step_sequential(self, n: int = 1):
+        """Advance every case n steps with plain per-case launches (the unbatched comparison)."""
         N.check(N.lib().mrlbm_batch_step_sequential(self._b, int(n)))
 
     def autotune(self, trial_steps: int = 3) -> tuple:
+        """Pick the fastest common tile height / z segment for the batch; state unchanged."""
         t = (C.c_int32 * 3)()
         N.check(N.lib().mrlbm_batch_autotune(self._b, int(trial_steps), t))
         for c in self.cases:
@@ -312,4 +337,5 @@ class Batch:
         return tuple(t)
 
     def sync(self):
+        """Wait for the batch's queued steps."""
         N.check(N.lib().mrlbm_batch_sync(self._b))
