@@ -65,3 +65,24 @@ def test_reference_arm_prints_once_under_torchrun(built):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["unit"] == "MLUPS"
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_shedding_statistics_of_a_known_signal():
+    """bench.shedding_stats on synthetic forces: constant drag plus a sinusoidal lift of known
+    amplitude and frequency gives back Cd, rms Cl and St (the C5 workload's statistics)."""
+    import math
+    import numpy as np
+    sys.path.insert(0, str(ROOT))
+    import bench
+    d, u, nz, n = 64.0, 0.05, 256, 38400  # second half: exactly 3 shedding periods
+    q = 0.5 * u * u * d * nz
+    t = np.arange(n)
+    st_true = 0.2
+    f = st_true * u / d  # shedding frequency per step
+    fx = 1.25 * q + 0.0 * t
+    fy = 0.3 * q * np.sin(2 * math.pi * f * t)
+    cd, cl_rms, st = bench.shedding_stats(fx, fy, d, u, nz)
+    assert abs(cd - 1.25) < 1e-12
+    assert abs(cl_rms - 0.3 / math.sqrt(2)) < 1e-9
+    assert abs(st - st_true) < 1e-9
+    assert all(math.isnan(v) for v in bench.shedding_stats(fx[:3], fy[:3], d, u, nz))
