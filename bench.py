@@ -132,24 +132,32 @@ def replica_value(n_nodes: int, steps: int, seconds: float, world: int) -> float
     return world * n_nodes * steps / seconds / 1e6
 
 
-def cpu_baseline(n: int, slab: int, steps: int, bits: int = 32):
-    """Oracle (CPU restatement of the reference step, FP32 or FP64) on an n x n x slab piece of
-    the TGV, all host threads."""
+def cpu_baseline(n: int, steps: int, bits: int = 64, budget_s: float = 20.0):
+    """The oracle (CPU restatement of the reference step; the reference has no CPU path) on the
+    full n^3 Taylor-Green grid of the workload, all host threads: one untimed step, then up to
+    `steps` timed steps, fewer if they would take longer than about `budget_s`.  The
+    descriptor is built without the solver library (oracle.periodic_box_desc)."""
     import oracle
-    from mrlbm_3d_cuda_gb300 import cases
-    from mrlbm_3d_cuda_gb300 import native as N
-    desc = cases.periodic_box(n, n, slab, u0=0.05, re=1600.0, length=n / (2 * math.pi))
+    desc = oracle.periodic_box_desc(n, 0.05, 1600.0)
     o = oracle.Oracle(desc, bits)
-    o.init(N.INIT_TAYLOR_GREEN, (0.05, n / (2 * math.pi)))
-    o.step(1)
+    o.init(2, (float(np.float32(0.05)), n / (2 * math.pi)))  # INIT_TAYLOR_GREEN
     t0 = time.perf_counter()
-    o.step(steps)
+    o.step(1)
+    first = time.perf_counter() - t0
+    k = max(1, min(steps, int(budget_s / max(first, 1e-3))))
+    t0 = time.perf_counter()
+    o.step(k)
     dt = time.perf_counter() - t0
     o.close()
     cores = os.cpu_count() or 1
-    return {"value": n * n * slab * steps / dt / 1e6, "unit": "MLUPS", "cores": cores, "kind": "port",
-            "sample": f"{steps} steps of a {n}x{n}x{slab} periodic slab of the same Taylor-Green field, "
-                      f"FP{bits} restatement, OpenMP {cores} threads"}
+    return {"value": n ** 3 * k / dt / 1e6, "unit": "MLUPS", "cores": cores, "kind": "port",
+            "sample": f"{k} time steps of the full {n}^3 Taylor-Green grid after one untimed step, "
+                      f"FP{bits} restatement of the reference step, OpenMP {cores} threads"}
+
+
+def watchdog_steps(first: int, k: int, every: int = 64) -> int:
+    """Steps it in [first, first + k) on which the divergence watchdog runs ((it + 1) % every == 0)."""
+    return (first + k) // every - first // every
 
 
 def metric_name(n: int) -> str:
@@ -157,40 +165,43 @@ def metric_name(n: int) -> str:
 
 
 def run_reference(args):
-    """The reference's algorithm on the host cores: the oracle (the reference has no CPU
-    path), one bounded n x n x slab piece of the same Taylor-Green field per step."""
+    """The reference's algorithm on the host cores: the FP32 oracle (the reference has no CPU
+    path) on the full n^3 Taylor-Green grid of the workload, all host threads.  Each timed
+    step is one full time step; the number of timed steps is K or fewer, so that the timed
+    steps take about --ref-budget seconds at most (the line says how many ran).  Only rank 0
+    runs; the descriptor is built without the solver library."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
     import oracle
-    from mrlbm_3d_cuda_gb300 import cases
-    from mrlbm_3d_cuda_gb300 import native as N
     n = args.n
-    slab = max(4, args.ref_slab)
-    desc = cases.periodic_box(n, n, slab, u0=0.05, re=1600.0, length=n / (2 * math.pi))
+    desc = oracle.periodic_box_desc(n, 0.05, 1600.0)
     o = oracle.Oracle(desc, 32)
-    o.init(N.INIT_TAYLOR_GREEN, (0.05, n / (2 * math.pi)))
-    for _ in range(args.warmup):
+    o.init(2, (float(np.float32(0.05)), n / (2 * math.pi)))  # INIT_TAYLOR_GREEN
+    t0 = time.perf_counter()
+    for _ in range(max(1, min(args.warmup, 3))):
         o.step(1)
+    per = (time.perf_counter() - t0) / max(1, min(args.warmup, 3))
+    k = max(1, min(args.steps, int(args.ref_budget / max(per, 1e-3))))
     times = []
-    for _ in range(args.steps):
+    for _ in range(k):
         t0 = time.perf_counter()
         o.step(1)
         times.append(time.perf_counter() - t0)
     o.close()
     total = sum(times)
-    value = n * n * slab * len(times) / total / 1e6 if total > 0 else 0.0
+    value = n ** 3 * len(times) / total / 1e6 if total > 0 else 0.0
     cores = os.cpu_count() or 1
+    sample = (f"{len(times)} full time steps of the {n}^3 Taylor-Green grid (of the {args.steps} asked, bounded "
+              f"to about {args.ref_budget:.0f} s) after {max(1, min(args.warmup, 3))} untimed ones, FP32 "
+              f"restatement of the reference step, OpenMP {cores} threads")
     line = {
         "impl": "reference", "metric": metric_name(n), "value": value, "unit": "MLUPS",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "n_gpus": world, "steps": args.steps, "steps_timed": len(times), "warmup": args.warmup,
         "ms_per_step": 1e3 * total / max(1, len(times)), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"taylor-green {n}^3 D3Q27, u0=0.05, Re=1600", "storage": "f32"},
-        "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": cores, "kind": "port",
-                         "sample": f"each step: one step of a {n}x{n}x{slab} periodic slab of the same "
-                                   f"Taylor-Green field, FP32 restatement of the reference step, "
-                                   f"OpenMP {cores} threads"},
+        "config": {"workload": f"taylor-green {n}^3 D3Q27, u0=0.05, Re=1600, full grid", "storage": "f32"},
+        "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -286,19 +297,14 @@ def run_batch(args):
 
 
 def shedding_stats(fx, fy, d, u, nz, rho0=1.0):
-    """Cd (mean), rms Cl and Strouhal number from per-step wall forces (second half of the run)."""
+    """Cd (mean), rms Cl and Strouhal number (lift zero crossings) from per-step wall forces,
+    over the second half of the run."""
+    from mrlbm_3d_cuda_gb300.statistics import shedding
     if len(fx) < 4:
         return float("nan"), float("nan"), float("nan")
     half = len(fx) // 2
-    q = 0.5 * rho0 * u * u * d * nz
-    cd = float(np.mean(fx[half:]) / q)
-    cl = fy[half:] / q
-    cl_rms = float(np.sqrt(np.mean((cl - cl.mean()) ** 2)))
-    spec = np.abs(np.fft.rfft(cl - cl.mean()))
-    freq = np.fft.rfftfreq(len(cl), d=1.0)
-    k = int(np.argmax(spec[1:]) + 1) if len(spec) > 1 else 0
-    st = float(freq[k] * d / u) if k else float("nan")
-    return cd, cl_rms, st
+    s = shedding(np.arange(len(fx) - half), fx[half:], fy[half:], d, u, nz, rho0)
+    return s.cd, s.cl_rms, s.st
 
 
 def run_c5(args):
@@ -507,15 +513,16 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "MLUPS", "h2d_bytes_per_step": hv.nbytes / e2e_steps,
                 "d2h_bytes_per_step": 16 + hv.nbytes / e2e_steps},
         # per step: the step kernel; the cylinder adds the boundary-tile step kernel, the
-        # node-list kernel and the wall kernel; stochastic rounding adds its counter tick
-        "gpu_launches": args.steps * ((4 if cyl else 1) + sr),
+        # node-list kernel and the wall kernel; stochastic rounding adds its counter tick; every
+        # 64th step (the divergence watchdog) adds the FP64 sum kernel
+        "gpu_launches": args.steps * ((4 if cyl else 1) + sr) + watchdog_steps(args.warmup, args.steps),
         "clocks": clk.summary(),
     }
     if not cyl and storage == "f32" and not args.no_storage_comparison:
         line["storage_comparison"] = storage_comparison(args, stream, args.n, world)
         line["storage_comparison"]["f32"]["value"] = value
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(min(args.n, 128), 8, args.cpu_steps, bits=64)
+        line["cpu_baseline"] = cpu_baseline(args.n, args.cpu_steps, bits=64)
     sim.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -540,7 +547,8 @@ def main():
     ap.add_argument("--c5-runs", default="f16,f32", help="storage runs of the c5 workload (f16 first: its speed is the value)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--diameter", type=int, default=16)
-    ap.add_argument("--ref-slab", type=int, default=8)
+    ap.add_argument("--ref-budget", type=float, default=60.0,
+                    help="--impl reference: seconds of timed full-grid CPU steps at most")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-storage-comparison", action="store_true",

@@ -133,7 +133,12 @@ typedef struct mrlbm_case_desc {
     int32_t stochastic_rounding; /* FP16 / BF16 only: 1 rounds the time-step stores
                                     stochastically (hardware cvt.rs with hashed random bits
                                     per node, field pair and step) instead of to nearest     */
-    int32_t reserved[15];
+    int32_t watchdog_every; /* divergence watchdog period in steps, independent of sampling:
+                               every this many steps the step computes its FP64 mass / energy
+                               sums on the device and flags non-finite ones, and mrlbm_step /
+                               mrlbm_sync return MRLBM_ERR_DIVERGED once the flag is seen;
+                               0: the default (64), < 0: off                               */
+    int32_t reserved[14];
 } mrlbm_case_desc;
 
 typedef struct mrlbm_info {

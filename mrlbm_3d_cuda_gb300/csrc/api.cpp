@@ -73,6 +73,9 @@ void free_all(mrlbm_handle *h) {
     f(h->d_tag);
     f(h->d_args);
     f(h->d_error);
+    f(h->d_watch);
+    if (h->h_status) cudaFreeHost(h->h_status);
+    h->h_status = nullptr;
     f(h->d_sr_step);
     f(h->d_force_ring);
     f(h->d_diag_ring);
@@ -101,6 +104,18 @@ int ensure_stage(mrlbm_handle *h, size_t bytes) {
     h->stage_bytes = 0;
     CK(h, cudaMalloc((void **)&h->d_stage, bytes));
     h->stage_bytes = bytes;
+    return MRLBM_OK;
+}
+
+// A new state (init, uploaded moments, loaded checkpoint) starts with a clear divergence flag.
+// The stream is drained first so that no queued watchdog copy lands after the clear.
+int clear_divergence(mrlbm_handle *h) {
+    CK(h, cudaStreamSynchronize(h->stream));
+    int e = 0;
+    CK(h, cudaMemcpy(&e, h->d_error, sizeof(int), cudaMemcpyDeviceToHost));
+    e &= ~kErrorDiverged;
+    CK(h, cudaMemcpy(h->d_error, &e, sizeof(int), cudaMemcpyHostToDevice));
+    *h->h_status = e;
     return MRLBM_OK;
 }
 
@@ -278,13 +293,23 @@ int setup_tiling(mrlbm_handle *h, int ty, int lz) {
 
 // One or more time steps of one handle: step kernel, node-list kernel, wall kernel and the
 // sampled force / diagnostics reductions, all asynchronous on the handle's stream.
+// The divergence flag as last copied back to the host (no synchronisation: the copy of a
+// watchdog step lands in the pinned word while later steps are queued).
+bool diverged_seen(const mrlbm_handle *h) {
+    return h->h_status && (*(const volatile int *)h->h_status & kErrorDiverged);
+}
+
 int step_handle(mrlbm_handle *h, int32_t nsteps) {
+    if (diverged_seen(h))
+        return fail(h, MRLBM_ERR_DIVERGED, "the divergence watchdog found non-finite mass / energy sums");
     const int nb = (int)(h->geo.wall[0].list.size() + h->geo.wall[1].list.size());
     const int nbf = (int)(h->geo.wall[0].fluid_list.size() + h->geo.wall[1].fluid_list.size());
     for (int s = 0; s < nsteps; ++s) {
         const int64_t it = h->step;
         const bool fs = h->force_every > 0 && it % h->force_every == 0;
         const bool ds = h->diag_every > 0 && it % h->diag_every == 0;
+        // watchdog steps compute the same sums as a sampled step, into their own slot
+        const bool ws = !ds && h->watchdog_every > 0 && (it + 1) % h->watchdog_every == 0;
         StepLaunch L;
         L.ga = h->d_args;
         L.parity = h->parity;
@@ -297,7 +322,8 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
             h->force_steps[slot] = it;
             ++h->force_count;
         }
-        if (ds) L.diag_part = h->d_diag_part;
+        const bool sums = ds || ws;
+        if (sums) L.diag_part = h->d_diag_part;
         const int n_step_parts = h->n_ctas + h->n_ctas_sp;
         // The boundary work of the step runs on the side stream, concurrently with the bulk
         // tiles: the boundary-tile step kernel, then the node-list kernel (it reads only the
@@ -309,14 +335,14 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
             StepLaunch Ls = L;
             Ls.ga = h->d_args_sp;
             Ls.n_ctas = h->n_ctas_sp;
-            Ls.diag_part = ds ? h->d_diag_part + 2 * h->n_ctas : nullptr;
+            Ls.diag_part = sums ? h->d_diag_part + 2 * h->n_ctas : nullptr;
             CK(h, cudaEventRecord(h->ev_fork, h->stream));
             CK(h, cudaStreamWaitEvent(h->side_stream, h->ev_fork, 0));
             CK(h, launch_step(Ls, h->storage, h->tile_y, true, h->side_stream));
             bs = h->side_stream;
         }
         if (h->n_list > 0)
-            CK(h, launch_special_list(L, h->storage, h->n_list_blocks, ds ? h->d_diag_part + 2 * n_step_parts : nullptr,
+            CK(h, launch_special_list(L, h->storage, h->n_list_blocks, sums ? h->d_diag_part + 2 * n_step_parts : nullptr,
                                       bs));
         if (nb > 0) CK(h, launch_wall(L, h->storage, nb + (fs ? nbf : 0), bs));
         if (h->n_items_sp > 0) CK(h, cudaEventRecord(h->ev_join, h->side_stream));
@@ -335,12 +361,17 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
                                               (int)h->geo.wall[w].list.size(), h->d_ps_avg[w], h->ps_count,
                                               h->stream));
         }
-        if (ds) {
-            const int64_t slot = h->diag_count % kRing;
-            CK(h, launch_diag_finalize(h->d_diag_part, n_step_parts + (h->n_list > 0 ? h->n_list_blocks : 0),
-                                       h->d_diag_ring + slot * 2, h->stream));
-            h->diag_steps[slot] = it;
-            ++h->diag_count;
+        if (sums) {
+            const int parts = n_step_parts + (h->n_list > 0 ? h->n_list_blocks : 0);
+            if (ds) {
+                const int64_t slot = h->diag_count % kRing;
+                CK(h, launch_diag_finalize(h->d_diag_part, parts, h->d_diag_ring + slot * 2, h->d_error, h->stream));
+                h->diag_steps[slot] = it;
+                ++h->diag_count;
+            } else {
+                CK(h, launch_diag_finalize(h->d_diag_part, parts, h->d_watch, h->d_error, h->stream));
+            }
+            CK(h, cudaMemcpyAsync(h->h_status, h->d_error, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
         }
         if (h->d_sr_step) CK(h, launch_sr_tick(h->d_sr_step, h->stream));
         h->parity ^= 1;
@@ -367,9 +398,7 @@ struct SavedState {
 };
 
 int save_state(mrlbm_handle *h, SavedState &st) {
-    const size_t bytes = (size_t)h->fs * h->vbytes;
-    CK(h, cudaMalloc(&st.buf, bytes));
-    CK(h, cudaMemcpyAsync(st.buf, h->m[h->parity], bytes, cudaMemcpyDeviceToDevice, h->stream));
+    // counters first: a failed save leaves them to restore_state unchanged
     st.parity = h->parity;
     st.force_every = h->force_every;
     st.diag_every = h->diag_every;
@@ -378,17 +407,25 @@ int save_state(mrlbm_handle *h, SavedState &st) {
     st.diag_count = h->diag_count;
     st.ps_start = h->ps_start;
     st.ps_end = h->ps_end;
+    const size_t bytes = (size_t)h->fs * h->vbytes;
+    CK(h, cudaMalloc(&st.buf, bytes));
+    CK(h, cudaMemcpyAsync(st.buf, h->m[h->parity], bytes, cudaMemcpyDeviceToDevice, h->stream));
     h->force_every = h->diag_every = 0;
     h->ps_start = h->ps_end = -1;  // no statistics-window samples from trial steps
     return MRLBM_OK;
 }
 
+// Put back what save_state kept (counters always; the field if it was saved) and free the copy.
 int restore_state(mrlbm_handle *h, SavedState &st) {
-    const size_t bytes = (size_t)h->fs * h->vbytes;
-    CK(h, cudaMemcpyAsync(h->m[st.parity], st.buf, bytes, cudaMemcpyDeviceToDevice, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
-    cudaFree(st.buf);
-    st.buf = nullptr;
+    int rc = MRLBM_OK;
+    if (st.buf) {
+        const size_t bytes = (size_t)h->fs * h->vbytes;
+        cudaError_t e = cudaMemcpyAsync(h->m[st.parity], st.buf, bytes, cudaMemcpyDeviceToDevice, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        cudaFree(st.buf);
+        st.buf = nullptr;
+        if (e != cudaSuccess) rc = cuda_fail(h, e, "restoring the saved field");
+    }
     h->parity = st.parity;
     h->force_every = st.force_every;
     h->diag_every = st.diag_every;
@@ -397,6 +434,7 @@ int restore_state(mrlbm_handle *h, SavedState &st) {
     h->diag_count = st.diag_count;
     h->ps_start = st.ps_start;
     h->ps_end = st.ps_end;
+    if (rc != MRLBM_OK) return rc;
     return sync_sr_step(h);
 }
 
@@ -611,6 +649,10 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     }
     CK(H, cudaMalloc((void **)&h->d_error, sizeof(int)));
     CK(H, cudaMemset(h->d_error, 0, sizeof(int)));
+    CK(H, cudaMalloc((void **)&h->d_watch, 2 * sizeof(double)));
+    CK(H, cudaHostAlloc((void **)&h->h_status, sizeof(int), cudaHostAllocDefault));
+    *h->h_status = 0;
+    h->watchdog_every = d.watchdog_every == 0 ? kWatchdogDefault : (d.watchdog_every < 0 ? 0 : d.watchdog_every);
     CK(H, cudaMalloc((void **)&h->d_force_ring, (size_t)kRing * 10 * sizeof(double)));
     CK(H, cudaMalloc((void **)&h->d_diag_ring, (size_t)kRing * 2 * sizeof(double)));
     h->force_steps.assign(kRing, -1);
@@ -732,6 +774,7 @@ int mrlbm_init(mrlbm_handle *h, int32_t kind, const double *params, int32_t n_pa
                      : kind == MRLBM_INIT_NOISY_UNIFORM ? 5 : 0;
     if (n_params < need || (need && !params)) return fail(h, MRLBM_ERR_INVALID_ARG, "missing init parameters");
     for (int k = 0; k < need && k < 8; ++k) ia.p[k] = params[k];
+    if (int rc = clear_divergence(h)) return rc;
     CK(h, launch_init(ia, h->storage, h->stream));
     h->parity = 0;
     h->step = 0;
@@ -759,6 +802,13 @@ int mrlbm_step(mrlbm_handle *h, int32_t nsteps) {
     return step_handle(h, nsteps);
 }
 
+// Test hook for the autotuners' failure paths: MRLBM_FAULT_AUTOTUNE_TRIAL=k makes trial k
+// (1-based) of every autotune call fail as a CUDA error would, on the host, before it launches.
+static int injected_trial_failure(int trial) {
+    const char *v = std::getenv("MRLBM_FAULT_AUTOTUNE_TRIAL");
+    return v && std::atoi(v) == trial;
+}
+
 int mrlbm_autotune(mrlbm_handle *h, int32_t trial_steps, int32_t tile_out[3]) {
     if (!h) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "null handle");
     if (h->host_only) return fail(h, MRLBM_ERR_STATE, "host-only handle has no device state");
@@ -766,33 +816,52 @@ int mrlbm_autotune(mrlbm_handle *h, int32_t trial_steps, int32_t tile_out[3]) {
     if (trial_steps < 1) return fail(h, MRLBM_ERR_INVALID_ARG, "need at least one trial step");
     SavedState st;
     int rc = save_state(h, st);
-    if (rc) return rc;
-    cudaEvent_t e0, e1;
-    CK(h, cudaEventCreate(&e0));
-    CK(h, cudaEventCreate(&e1));
+    if (rc) {
+        if (st.buf) cudaFree(st.buf);
+        return rc;
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const int ty0 = h->tile_y, lz0 = h->lz;
     float best = 1e30f;
-    int best_ty = h->tile_y, best_lz = h->lz;
-    for (int ty : {4, 8, 16}) {
-        for (int lz : lz_candidates(h->d.nz)) {
-            if ((rc = setup_tiling(h, ty, lz)) != MRLBM_OK) return rc;
-            if ((rc = step_handle(h, 1)) != MRLBM_OK) return rc;  // warm-up
-            CK(h, cudaEventRecord(e0, h->stream));
-            if ((rc = step_handle(h, trial_steps)) != MRLBM_OK) return rc;
-            CK(h, cudaEventRecord(e1, h->stream));
-            CK(h, cudaEventSynchronize(e1));
-            float ms = 0.f;
-            CK(h, cudaEventElapsedTime(&ms, e0, e1));
-            if (ms < best) {
-                best = ms;
-                best_ty = ty;
-                best_lz = h->lz;
+    int best_ty = ty0, best_lz = lz0;
+    // the trials; any failure leaves the loop with its status and falls through to the
+    // clean-up below, which always runs
+    auto trials = [&]() -> int {
+        CK(h, cudaEventCreate(&e0));
+        CK(h, cudaEventCreate(&e1));
+        int trial = 0, r;
+        for (int ty : {4, 8, 16}) {
+            for (int lz : lz_candidates(h->d.nz)) {
+                if (injected_trial_failure(++trial))
+                    return fail(h, MRLBM_ERR_CUDA, "autotune trial " + std::to_string(trial) + ": injected failure");
+                if ((r = setup_tiling(h, ty, lz)) != MRLBM_OK) return r;
+                if ((r = step_handle(h, 1)) != MRLBM_OK) return r;  // warm-up
+                CK(h, cudaEventRecord(e0, h->stream));
+                if ((r = step_handle(h, trial_steps)) != MRLBM_OK) return r;
+                CK(h, cudaEventRecord(e1, h->stream));
+                CK(h, cudaEventSynchronize(e1));
+                float ms = 0.f;
+                CK(h, cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    best_ty = ty;
+                    best_lz = h->lz;
+                }
             }
         }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if ((rc = setup_tiling(h, best_ty, best_lz)) != MRLBM_OK) return rc;
-    if ((rc = restore_state(h, st)) != MRLBM_OK) return rc;
+        return MRLBM_OK;
+    };
+    rc = trials();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    // keep the fastest tiling, or the one in use before a failed search; then the saved state
+    std::string first_err = rc != MRLBM_OK ? h->err : std::string();
+    int r2 = setup_tiling(h, rc == MRLBM_OK ? best_ty : ty0, rc == MRLBM_OK ? best_lz : lz0);
+    int r3 = restore_state(h, st);
+    if (st.buf) cudaFree(st.buf);
+    if (rc != MRLBM_OK) return fail(h, rc, first_err);
+    if (r2 != MRLBM_OK) return r2;
+    if (r3 != MRLBM_OK) return r3;
     if (tile_out) {
         tile_out[0] = TILE_X;
         tile_out[1] = h->tile_y;
@@ -807,7 +876,11 @@ int mrlbm_sync(mrlbm_handle *h) {
     CK(h, cudaStreamSynchronize(h->stream));
     int e = 0;
     CK(h, cudaMemcpy(&e, h->d_error, sizeof(int), cudaMemcpyDeviceToHost));
-    if (e) return fail(h, MRLBM_ERR_CUDA, "device reported a stencil lookup failure (code " + std::to_string(e) + ")");
+    *h->h_status = e;
+    if (e & ~kErrorDiverged)
+        return fail(h, MRLBM_ERR_CUDA, "device reported a stencil lookup failure (code " + std::to_string(e) + ")");
+    if (e & kErrorDiverged)
+        return fail(h, MRLBM_ERR_DIVERGED, "the divergence watchdog found non-finite mass / energy sums");
     if (h->diag_count > 0) {
         double v[2];
         const int64_t slot = (h->diag_count - 1) % kRing;
@@ -850,6 +923,7 @@ int mrlbm_set_moments(mrlbm_handle *h, uint32_t mask, int32_t layout, const floa
     void *cur = h->m[h->parity], *oth = h->m[h->parity ^ 1];
     int rc = ensure_stage(h, (size_t)nf * h->n * 4);
     if (rc) return rc;
+    if ((rc = clear_divergence(h)) != MRLBM_OK) return rc;
     CK(h, cudaMemcpyAsync(h->d_stage, host, (size_t)nf * h->n * 4, cudaMemcpyHostToDevice, h->stream));
     CK(h, launch_convert(nullptr, cur, oth, h->d_stage, mask, layout, h->d.nx, h->d.ny, h->d.nz, h->storage, h->sc, 1,
                          h->stream));
@@ -1293,44 +1367,73 @@ int mrlbm_batch_autotune(mrlbm_batch *b, int32_t trial_steps, int32_t tile_out[3
     if (trial_steps < 1) return bfail(MRLBM_ERR_INVALID_ARG, "need at least one trial step");
     BCK(cudaStreamSynchronize(b->stream));
     std::vector<SavedState> saved(b->h.size());
+    auto release = [&]() {
+        for (SavedState &st : saved)
+            if (st.buf) {
+                cudaFree(st.buf);
+                st.buf = nullptr;
+            }
+    };
     for (size_t c = 0; c < b->h.size(); ++c)
-        if ((rc = save_state(b->h[c], saved[c])) != MRLBM_OK) return rc;
+        if ((rc = save_state(b->h[c], saved[c])) != MRLBM_OK) {
+            // cases saved so far get their sampling back; nothing has stepped yet
+            for (size_t k = 0; k <= c; ++k) restore_state(b->h[k], saved[k]);
+            release();
+            return rc;
+        }
     const int saved_parity = b->parity, saved_force = b->force_every;
     const int64_t saved_step = b->step;
+    const int ty0 = b->tile_y, lz0 = b->lz;
     b->force_every = 0;
-    cudaEvent_t e0, e1;
-    BCK(cudaEventCreate(&e0));
-    BCK(cudaEventCreate(&e1));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
     int max_nz = 0;
     for (mrlbm_handle *h : b->h) max_nz = std::max(max_nz, h->d.nz);
     float best = 1e30f;
-    int best_ty = b->tile_y, best_lz = b->lz;
-    for (int ty : {4, 8, 16}) {
-        for (int lz : lz_candidates(max_nz)) {
-            if ((rc = batch_set_tiling(b, ty, lz)) != MRLBM_OK) return rc;
-            if ((rc = batch_step_once(b, false)) != MRLBM_OK) return rc;  // warm-up
-            BCK(cudaEventRecord(e0, b->stream));
-            for (int s = 0; s < trial_steps; ++s)
-                if ((rc = batch_step_once(b, false)) != MRLBM_OK) return rc;
-            BCK(cudaEventRecord(e1, b->stream));
-            BCK(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            BCK(cudaEventElapsedTime(&ms, e0, e1));
-            if (ms < best) {
-                best = ms;
-                best_ty = ty;
-                best_lz = lz;
+    int best_ty = ty0, best_lz = lz0;
+    auto trials = [&]() -> int {
+        BCK(cudaEventCreate(&e0));
+        BCK(cudaEventCreate(&e1));
+        int trial = 0, r;
+        for (int ty : {4, 8, 16}) {
+            for (int lz : lz_candidates(max_nz)) {
+                if (injected_trial_failure(++trial))
+                    return bfail(MRLBM_ERR_CUDA, "batch autotune trial " + std::to_string(trial) + ": injected failure");
+                if ((r = batch_set_tiling(b, ty, lz)) != MRLBM_OK) return r;
+                if ((r = batch_step_once(b, false)) != MRLBM_OK) return r;  // warm-up
+                BCK(cudaEventRecord(e0, b->stream));
+                for (int s = 0; s < trial_steps; ++s)
+                    if ((r = batch_step_once(b, false)) != MRLBM_OK) return r;
+                BCK(cudaEventRecord(e1, b->stream));
+                BCK(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                BCK(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    best_ty = ty;
+                    best_lz = lz;
+                }
             }
         }
+        return MRLBM_OK;
+    };
+    rc = trials();
+    const std::string first_err = rc != MRLBM_OK ? mrlbm::g_last_error : std::string();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamSynchronize(b->stream);
+    int r2 = batch_set_tiling(b, rc == MRLBM_OK ? best_ty : ty0, rc == MRLBM_OK ? best_lz : lz0);
+    int r3 = MRLBM_OK;
+    for (size_t c = 0; c < b->h.size(); ++c) {
+        const int r = restore_state(b->h[c], saved[c]);
+        if (r != MRLBM_OK && r3 == MRLBM_OK) r3 = r;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if ((rc = batch_set_tiling(b, best_ty, best_lz)) != MRLBM_OK) return rc;
-    for (size_t c = 0; c < b->h.size(); ++c)
-        if ((rc = restore_state(b->h[c], saved[c])) != MRLBM_OK) return rc;
+    release();
     b->parity = saved_parity;
     b->step = saved_step;
     b->force_every = saved_force;
+    if (rc != MRLBM_OK) return bfail(rc, first_err);
+    if (r2 != MRLBM_OK) return r2;
+    if (r3 != MRLBM_OK) return r3;
     if (tile_out) {
         tile_out[0] = TILE_X;
         tile_out[1] = b->tile_y;

@@ -15,6 +15,7 @@
 namespace mrlbm {
 extern thread_local std::string g_last_error;
 constexpr int kRing = 65536;  // sampled steps kept on the device (forces, diagnostics)
+constexpr int kWatchdogDefault = 64;  // steps between divergence checks unless the case sets it
 }  // namespace mrlbm
 
 using mrlbm::BatchArgs;
@@ -66,6 +67,12 @@ struct mrlbm_handle {
     std::vector<int32_t> h_items, h_items_sp;  // host copies of the two work-item lists
     mrlbm_batch *batch = nullptr;   // owning batch, if any
     int *d_error = nullptr;
+    // divergence watchdog: every watchdog_every steps (0: off) the step computes its FP64 mass /
+    // energy sums into d_watch and flags non-finite ones in the error word, whose value is then
+    // copied to the pinned word h_status; mrlbm_step reads h_status without a synchronisation
+    int watchdog_every = 0;
+    double *d_watch = nullptr;
+    int *h_status = nullptr;
     uint32_t *d_sr_step = nullptr;  // stochastic-rounding step counter (16-bit storage with it on)
     // sampling
     int force_every = 0, diag_every = 0;
@@ -122,6 +129,8 @@ int cuda_fail(mrlbm_handle *h, cudaError_t e, const char *what);
 int ensure_stage(mrlbm_handle *h, size_t bytes);
 // Set the stochastic-rounding step counter to the handle's step (after init, load, restore).
 int sync_sr_step(mrlbm_handle *h);
+// Clear the divergence flag of the device error word and its host copy (new state).
+int clear_divergence(mrlbm_handle *h);
 }  // namespace mrlbm
 
 #define CK(h, call)                                                    \

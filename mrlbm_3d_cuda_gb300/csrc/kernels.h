@@ -123,8 +123,10 @@ cudaError_t launch_wall(const StepLaunch &l, int storage, int n_total, cudaStrea
 // Closures, stencil snapshots and collision of the listed non-bulk nodes (after launch_step).
 int special_list_blocks(int n_list);
 cudaError_t launch_special_list(const StepLaunch &l, int storage, int n_blocks, double *diag_part, cudaStream_t s);
-// Sum the per-CTA diagnostics partials into out[2] in a fixed order.
-cudaError_t launch_diag_finalize(const double *part, int n, double *out, cudaStream_t s);
+// Sum the per-CTA diagnostics partials into out[2] in a fixed order; a non-finite sum sets
+// kErrorDiverged in *error (if given).
+constexpr int kErrorDiverged = 16;
+cudaError_t launch_diag_finalize(const double *part, int n, double *out, int *error, cudaStream_t s);
 
 struct InitArgs {
     void *m_a = nullptr, *m_b = nullptr;  // both ping-pong buffers

@@ -15,6 +15,7 @@
 // node's 27 pulled populations come from planes z-1, z, z+1 without any population array in
 // HBM.  Post-collision moments go to the second ping-pong buffer.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -483,7 +484,8 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     }
 }
 
-__global__ void diag_finalize_kernel(const double *__restrict__ part, int n, double *__restrict__ out) {
+__global__ void diag_finalize_kernel(const double *__restrict__ part, int n, double *__restrict__ out,
+                                     int *__restrict__ error) {
     __shared__ double s[2][256];
     double a = 0.0, b = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -503,20 +505,25 @@ __global__ void diag_finalize_kernel(const double *__restrict__ part, int n, dou
     if (threadIdx.x == 0) {
         out[0] = s[0][0];
         out[1] = s[1][0];
+        if (error && !(isfinite(s[0][0]) && isfinite(s[1][0]))) atomicOr(error, kErrorDiverged);
     }
 }
 
-// Opt the kernel into its dynamic shared memory once per process (never inside a stream capture:
-// batched launches are prepared before their graphs are captured).
+// Opt the kernel into its dynamic shared memory once per device (the attribute belongs to the
+// current device's context; never set inside a stream capture: batched launches are prepared
+// before their graphs are captured).  Devices past the 64th are configured on every launch.
 template <typename S, int TY, bool SP, bool BATCH, bool FULL = false>
 cudaError_t configure_t() {
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(step_kernel<S, TY, SP, BATCH, FULL>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, Geo<TY>::SMEM);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0ull};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = dev >= 0 && dev < 64 ? 1ull << dev : 0ull;
+    if (bit && (configured.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(step_kernel<S, TY, SP, BATCH, FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             Geo<TY>::SMEM);
+    if (e != cudaSuccess) return e;
+    configured.fetch_or(bit, std::memory_order_acq_rel);
     return cudaSuccess;
 }
 
@@ -636,8 +643,8 @@ cudaError_t launch_step_batch(const BatchArgs *ba, int parity, int storage, int 
     }
 }
 
-cudaError_t launch_diag_finalize(const double *part, int n, double *out, cudaStream_t s) {
-    diag_finalize_kernel<<<1, 256, 0, s>>>(part, n, out);
+cudaError_t launch_diag_finalize(const double *part, int n, double *out, int *error, cudaStream_t s) {
+    diag_finalize_kernel<<<1, 256, 0, s>>>(part, n, out, error);
     return cudaGetLastError();
 }
 
@@ -674,7 +681,13 @@ namespace {
 
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
-void *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+// per device, set up on its first call: the scratch array's device address, the SM count and
+// the resident step-kernel CTAs per SM
+struct NoAllocDevice {
+    void *scratch = nullptr;
+    int n_sm = 0, per_sm = 0;
+};
+NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
 
 // Write the argument block, clear the error word and fill the work items (every xy tile of
 // every z segment, segment-major) inside the scratch array: one launch, no host staging.
@@ -689,16 +702,23 @@ __global__ void noalloc_setup_kernel(const StepArgs a, unsigned char *scratch, i
     for (int j = i; j < n_items; j += gridDim.x * blockDim.x) items[j] = (j % tiles) | ((j / tiles) << 20);
 }
 
-// Device address of the scratch array on the current device, looked up once per device.
-cudaError_t noalloc_scratch(int dev, unsigned char **out) {
+// Set-up of device `dev` (the current device), once: the scratch array's device address (in
+// host code the array's name is only a host-side stand-in), its SM count and the step kernel's
+// occupancy.  Host-side queries only; nothing is allocated.
+cudaError_t noalloc_device(int dev, NoAllocDevice &out) {
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    NoAllocDevice &d = g_noalloc_dev[dev];
+    if (!d.scratch) {
         void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
-        g_noalloc_ptr[dev] = p;
+        int n_sm = 0;
+        if ((e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        d.n_sm = n_sm;
+        d.per_sm = std::max(1, occ_s<float>(kNoAllocTileY));
+        d.scratch = p;
     }
-    *out = (unsigned char *)g_noalloc_ptr[dev];
+    out = d;
     return cudaSuccess;
 }
 
@@ -746,31 +766,34 @@ int noalloc_periodic_step(const NoAllocStep &p, std::string &err) {
         return MRLBM_ERR_INVALID_ARG;
     }
 
-    int dev = 0, major = 0, minor = 0, n_sm = 0;
+    int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return noalloc_cuda_fail(e, "cudaGetDevice", err);
     if (dev < 0 || dev >= kNoAllocMaxDevices) {
         err = std::string(fn) + "device ordinal out of range";
         return MRLBM_ERR_UNSUPPORTED;
     }
-    if ((e = cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev)) != cudaSuccess ||
-        (e = cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev)) != cudaSuccess ||
-        (e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
-        return noalloc_cuda_fail(e, "cudaDeviceGetAttribute", err);
-    if (!(major == 10 && minor == 3)) {
-        err = std::string(fn) + "libmrlbm is built for sm_103a (GB300) only";
-        return MRLBM_ERR_UNSUPPORTED;
+    NoAllocDevice nd;
+    if (!g_noalloc_dev[dev].scratch) {
+        int major = 0, minor = 0;
+        if ((e = cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev)) != cudaSuccess ||
+            (e = cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev)) != cudaSuccess)
+            return noalloc_cuda_fail(e, "cudaDeviceGetAttribute", err);
+        if (!(major == 10 && minor == 3)) {
+            err = std::string(fn) + "libmrlbm is built for sm_103a (GB300) only";
+            return MRLBM_ERR_UNSUPPORTED;
+        }
     }
-    unsigned char *scratch = nullptr;
-    if ((e = noalloc_scratch(dev, &scratch)) != cudaSuccess) return noalloc_cuda_fail(e, "cudaGetSymbolAddress", err);
+    if ((e = noalloc_device(dev, nd)) != cudaSuccess) return noalloc_cuda_fail(e, "device set-up", err);
+    unsigned char *scratch = (unsigned char *)nd.scratch;
 
     // tiling: 32 x 16 columns; the longest z segment that still gives every resident CTA
-    // several items, lengthened if the item list would not fit the scratch
-    const int per_sm = std::max(1, occ_s<float>(kNoAllocTileY));
-    const int resident = per_sm * n_sm;
+    // several items, lengthened if the item list would not fit the scratch or the segment
+    // number its 11-bit field of the work item (tile | segment << 20)
+    const int resident = nd.per_sm * nd.n_sm;
     int lz = p.nz;
     while (lz > 16 && (int64_t)tiles * ((p.nz + lz - 1) / lz) < 4LL * resident) lz = (lz + 1) / 2;
-    const int max_seg = kNoAllocMaxItems / tiles;
+    const int max_seg = std::min(kNoAllocMaxItems / tiles, 1 << 11);
     if ((p.nz + lz - 1) / lz > max_seg) lz = (p.nz + max_seg - 1) / max_seg;
     const int nseg = (p.nz + lz - 1) / lz;
     const int n_items = tiles * nseg;
@@ -808,7 +831,7 @@ int noalloc_periodic_step(const NoAllocStep &p, std::string &err) {
         cudaSuccess)
         return noalloc_cuda_fail(e, "step launch", err);
     if (p.diag_host) {
-        if ((e = launch_diag_finalize(part, n_ctas, sums, p.stream)) != cudaSuccess)
+        if ((e = launch_diag_finalize(part, n_ctas, sums, nullptr, p.stream)) != cudaSuccess)
             return noalloc_cuda_fail(e, "diagnostics launch", err);
         double v[2];
         if ((e = cudaMemcpyAsync(v, sums, sizeof(v), cudaMemcpyDeviceToHost, p.stream)) != cudaSuccess ||

@@ -51,7 +51,8 @@ class CaseDesc(C.Structure):
         ("storage", C.c_int32),
         ("storage_scale", C.c_float * 3),
         ("stochastic_rounding", C.c_int32),
-        ("reserved", C.c_int32 * 15),
+        ("watchdog_every", C.c_int32),
+        ("reserved", C.c_int32 * 14),
     ]
 
 

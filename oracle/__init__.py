@@ -37,8 +37,36 @@ def lib():
         L.oracle_wall_size.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.oracle_get_boundary.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.oracle_last_error.restype = C.c_char_p
+        L.oracle_omega.restype = C.c_float
+        L.oracle_omega.argtypes = [C.c_void_p]
         _lib = L
     return _lib
+
+
+def omega(desc) -> float:
+    """The oracle's own relaxation rate for `desc` (the reference's tau chain restated from the
+    descriptor's u_max, Re and length scale; an explicit omega when Re is not set)."""
+    return float(lib().oracle_omega(C.byref(desc)))
+
+
+def periodic_box_desc(n: int, u0: float = 0.05, re: float = 1600.0):
+    """Descriptor of the all-periodic n^3 Taylor-Green box (L = n / 2 pi), filled here without
+    the solver library: the CPU legs of bench.py run on it without loading libmrlbm.so.  Only
+    the fields the oracle reads are set; the relaxation rate is the oracle's own."""
+    import math
+
+    from mrlbm_3d_cuda_gb300.native import CaseDesc, GEOM_NONE
+    d = CaseDesc()
+    d.struct_size = C.sizeof(CaseDesc)
+    d.geometry = GEOM_NONE
+    d.nx = d.ny = d.nz = int(n)
+    d.periodic[0] = d.periodic[1] = d.periodic[2] = 1
+    d.u_max, d.rho0, d.re = float(u0), 1.0, float(re)
+    d.length = float(n / (2.0 * math.pi))
+    d.omega = 0.0
+    for k in range(3):
+        d.storage_scale[k] = 1.0
+    return d
 
 
 class Oracle:

@@ -1098,6 +1098,33 @@ Oracle<T> *as(void *p) {
     return (Oracle<T> *)((Any *)p)->o;
 }
 
+// Relaxation rate from the physical parameters, restating the reference's constexpr chains
+// (float VISC, TAU = 0.5 + 3 VISC evaluated in double and stored as float, OMEGA = 1 / TAU in
+// double stored as float):
+//   cylinder  VISC = U_MAX * D_WALL / RE                 MRLBM_3D/src/cases/cylinder/constants.cuh:52-54
+//   annulus   VISC = U_REL * GAP / RE, as2 = 3 (float)   MRLBM_3D/src/cases/annulus/constants.cuh:73-81
+//   box       VISC = U_MAX * L / RE (the Taylor-Green length L = N / 2 pi)
+// This is the oracle's own derivation, independent of the product's descriptor code.  A
+// descriptor without a Reynolds number carries an explicit relaxation rate instead.
+float reference_omega(const mrlbm_case_desc &d) {
+    if (!(d.re > 0.f)) return d.omega;
+    float visc;
+    double tau;
+    if (d.geometry == MRLBM_GEOM_ANNULUS) {
+        const float r_in = 0.5f * d.d_wall[0], r_out = 0.5f * d.d_wall[1];
+        const float u_rel = std::fabs(d.wall_u[0][1] - d.wall_u[1][1]);
+        visc = u_rel * (r_out - r_in) / d.re;
+        const float as2 = 3.0f;
+        tau = 0.5 + (double)(as2 * visc);
+    } else {
+        const float len = d.geometry == MRLBM_GEOM_CYLINDER ? d.d_wall[0] : d.length;
+        visc = d.u_max * len / d.re;
+        tau = 0.5 + 3.0 * (double)visc;
+    }
+    const float tau_f = (float)tau;
+    return (float)(1.0 / (double)tau_f);
+}
+
 template <typename T>
 void *make(const mrlbm_case_desc *d) {
     auto *o = new Oracle<T>();
@@ -1106,7 +1133,7 @@ void *make(const mrlbm_case_desc *d) {
     o->ny = d->ny;
     o->nz = d->nz;
     o->n = (int64_t)d->nx * d->ny * d->nz;
-    o->omega = (T)d->omega;
+    o->omega = (T)reference_omega(*d);
     o->rho0 = (T)d->rho0;
     o->umax = (T)d->u_max;
     const std::string e = o->geometry();
@@ -1137,10 +1164,18 @@ extern "C" {
 
 const char *oracle_last_error(void) { return g_err.c_str(); }
 
-// d must be finalized (omega set) by the caller.  bits = 32 (float) or 64 (double).
+float oracle_omega(const mrlbm_case_desc *d) { return d ? reference_omega(*d) : 0.f; }
+
+// The relaxation rate comes from reference_omega (re > 0) or the descriptor's explicit omega.
+// bits = 32 (float) or 64 (double).
 void *oracle_create(const mrlbm_case_desc *d, int bits) {
-    if (!d || d->omega <= 0.f || d->nx % 8 || d->ny % 8 || d->nz % 4) {
-        g_err = "bad descriptor (finalize it first)";
+    if (!d || d->nx <= 0 || d->ny <= 0 || d->nz <= 0 || d->nx % 8 || d->ny % 8 || d->nz % 4) {
+        g_err = "bad descriptor (grid must be positive multiples of 8 x 8 x 4)";
+        return nullptr;
+    }
+    const float om = reference_omega(*d);
+    if (!(om > 0.f && om < 2.f)) {
+        g_err = "bad descriptor: no Reynolds number and no relaxation rate in (0, 2)";
         return nullptr;
     }
     void *o = bits == 32 ? make<float>(d) : make<double>(d);

@@ -4,6 +4,8 @@ Markers: `gpu` — needs a GB300 (sm_103a); everything else runs on the CPU.  Th
 library and the oracle are built in-tree on first use (incremental)."""
 from __future__ import annotations
 
+import json
+import os
 import sys
 from pathlib import Path
 
@@ -62,3 +64,26 @@ def field_errors(a: np.ndarray, b: np.ndarray, u_ref: float):
         out.append((d.max() / max(binf, sc[k]), d.max() / binf if binf > 0 else d.max(),
                     np.linalg.norm(a[k] - b[k]) / max(np.linalg.norm(b[k]), 1e-300)))
     return np.array(out)
+
+
+FIELD_NAMES = ("rho", "ux", "uy", "uz", "mxx", "myy", "mzz", "mxy", "mxz", "myz")
+_PARITY_LOG: dict = {}
+
+
+def record_parity(name: str, err: np.ndarray, **extra):
+    """Keep one test's per-field errors (rows of field_errors: floored, plain, L2) for the
+    parity report that MRLBM_PARITY_REPORT=<path> asks for at the end of the session."""
+    err = np.asarray(err)
+    _PARITY_LOG[name] = {
+        "floored": {f: float(err[k, 0]) for k, f in enumerate(FIELD_NAMES)},
+        "plain": {f: float(err[k, 1]) for k, f in enumerate(FIELD_NAMES)},
+        "l2": {f: float(err[k, 2]) for k, f in enumerate(FIELD_NAMES)},
+        **{k: (v.tolist() if isinstance(v, np.ndarray) else v) for k, v in extra.items()},
+    }
+
+
+def pytest_sessionfinish(session, exitstatus):
+    path = os.environ.get("MRLBM_PARITY_REPORT")
+    if path and _PARITY_LOG:
+        Path(path).parent.mkdir(parents=True, exist_ok=True)
+        Path(path).write_text(json.dumps(_PARITY_LOG, indent=1, sort_keys=True))

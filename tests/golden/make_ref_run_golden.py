@@ -1,29 +1,38 @@
-"""Golden vectors from a run of the reference's own GPU build (sakthi-lbm/MRLBM_3D_CUDA).
+"""Golden vectors from runs of the reference's own GPU build (sakthi-lbm/MRLBM_3D_CUDA).
 
 The reference ships no test data, so the time step is pinned against its own solver run on
-a GB300: `oracle/ref_gpu.py` stages, builds and runs the shipped cylinder case
-(cases/cylinder/constants.cuh: 336 x 144 x 48, D = 16, Re = 100, U = 0.1, periodic y and z,
-convective outlet) for MAX_ITER = N, i.e. iterations 0..N = N + 1 steps from the reference
-initial state.  Its checkpoint (restart.bin, MRLBM_3D/src/restart/restart_io.cu:3-52:
-int iteration, then rho - rho0, ux, uy, uz, mxx, myy, mzz, mxy, mxz, myz, each NX*NY*NZ
-floats in the tiled IDX_BLOCK order) and forces.dat (stat_header.cuh:16-33: `iter Fx Fy Fz`
-per step) are reduced here to a fixture small enough to commit:
-  * every node that is not plain bulk fluid (walls, BCFLUID, inlet / outlet faces) plus a
-    seeded random sample of 40,000 nodes, all 10 moments, by tiled index; with z walls
-    (stage --z-walls, Z_PERIODIC 0) the plain z-face nodes are sampled (8,000 of them)
-    except inside the classification window, which is kept whole on the two outer planes
-    at each end (BCSOLID nodes and their neighbours);
-  * per-field max |m|, sum m and sum m^2 over the whole grid (FP64);
-  * the forces.dat rows;
-  * 5,000 seeded positions of each of the six face-population arrays that follow the moments
-    in restart.bin (X_WEST, X_EAST, Y_SOUTH, Y_NORTH, Z_BACK, Z_FRONT, core/index.cuh:42-79),
-    with their values.
+a GB300: `oracle/ref_gpu.py` stages, builds and runs it, and this script reduces the run's
+output to a fixture small enough to commit.  The reference writes
 
-Run on the GPU machine from the repository root:
-    python oracle/ref_gpu.py stage cyl_n10 --steps 10          (where the reference tree is)
-    python oracle/ref_gpu.py check && python oracle/ref_gpu.py build cyl_n10 && python oracle/ref_gpu.py run cyl_n10
-    python tests/golden/make_ref_run_golden.py cyl_n10 tests/golden/ref_cylinder_run_n10.npz
-(z walls: stage cylz_n10 --steps 10 --z-walls, output ref_cylinder_zwall_run_n10.npz).
+  * restart.bin (MRLBM_3D/src/restart/restart_io.cu:3-52): int iteration, then rho - rho0,
+    ux, uy, uz, mxx, myy, mzz, mxy, mxz, myz, each NX*NY*NZ floats in the tiled IDX_BLOCK
+    order (core/index.cuh:11-28), then the six face-population arrays (X_WEST, X_EAST,
+    Y_SOUTH, Y_NORTH, Z_BACK, Z_FRONT, core/index.cuh:42-79);
+  * forces.dat (statistics/stat_header.cuh:16-33): `iter Fx Fy Fz` per step of the statistics
+    window;
+  * pressure.dat (cases/cylinder/cylinder_kernels.cu:238-283): `theta z Cp`;
+  * `REF_LOOP_MS <ms> REF_LOOP_STEPS <n>` on stdout (the staged copy's loop timer).
+
+Kinds (the staged case, from baseline/_ref/<tag>/config.json):
+
+  cylinder  the shipped cylinder case (336 x 144 x 48, D = 16, Re = 100, U = 0.1, periodic y
+            and z, convective outlet) after N + 1 steps: every node that is not plain bulk
+            fluid plus 40,000 random nodes, all 10 moments; with z walls the plain z-face
+            nodes are sampled (8,000) except inside the classification window, kept whole on
+            the two outer planes at each end; per-field max |m|, sum m, sum m^2 (FP64); the
+            forces.dat rows; 5,000 positions of each face-population array.
+  shedding  the shipped cylinder case run as shipped (56,000 steps, forces.dat over
+            iterations 48,000..56,000), one or more runs of the same build: every run's
+            forces.dat rows, pressure.dat and loop time.
+  annulus   the shipped annulus (136 x 136 x 256, r = 32 / 64, inner wall 0.03, Re = 70)
+            after N + 1 steps: every non-bulk node (both walls, BCFLUID) of the planes
+            z = 0, 1, 2, 128, 253, 254, 255, 20,000 further random non-bulk nodes and 40,000
+            random nodes, all 10 moments; field statistics as above.
+  tgv       the Taylor-Green vortex on the n^3 periodic grid after N + 1 steps: 40,000 random
+            nodes and the whole y = 0 plane, all 10 moments; field statistics; loop time.
+
+Run on the GPU machine from the repository root (after oracle/ref_gpu.py build/run):
+    python tests/golden/make_ref_run_golden.py <tag> <out.npz>
 """
 from __future__ import annotations
 
@@ -47,11 +56,50 @@ def read_restart(path: Path, n: int):
     return it, m, halo
 
 
-def main(tag: str, out: str):
-    from mrlbm_3d_cuda_gb300 import Simulation, cases
+def tiled_to_lex(idx: np.ndarray, nx: int, ny: int, nz: int) -> np.ndarray:
+    """Reference tiled IDX_BLOCK index (8 x 8 x 4 blocks) -> x + nx (y + ny z)."""
+    idx = idx.astype(np.int64)
+    gx, gy = nx // 8, ny // 8
+    block, thread = idx // 256, idx % 256
+    bx, by, bz = block % gx, (block // gx) % gy, block // (gx * gy)
+    x, y, z = bx * 8 + thread % 8, by * 8 + (thread // 8) % 8, bz * 4 + thread // 64
+    return x + nx * (y + ny * z)
+
+
+def lex_to_tiled(lex: np.ndarray, nx: int, ny: int) -> np.ndarray:
+    lex = lex.astype(np.int64)
+    x, y, z = lex % nx, (lex // nx) % ny, lex // (nx * ny)
+    gx, gy = nx // 8, ny // 8
+    block = (x // 8) + gx * ((y // 8) + gy * (z // 4))
+    return block * 256 + (x % 8) + 8 * (y % 8) + 64 * (z % 4)
+
+
+def field_stats(m: np.ndarray) -> dict:
+    m64 = m.astype(np.float64)
+    return {"field_max": np.abs(m64).max(axis=1), "field_sum": m64.sum(axis=1),
+            "field_sumsq": (m64 * m64).sum(axis=1)}
+
+
+def loop_time(run_dir: Path) -> np.ndarray:
+    p = run_dir / "loop_time.json"
+    if not p.exists():
+        return np.array([np.nan, 0.0])
+    t = json.loads(p.read_text())
+    return np.array([t["ms"], float(t["steps"])])
+
+
+def node_classes(desc, layout_tiled: bool = True) -> np.ndarray:
+    from mrlbm_3d_cuda_gb300 import Simulation
     from mrlbm_3d_cuda_gb300 import native as N
-    d = ROOT / "baseline" / "_ref" / tag
-    cfg = json.loads((d / "config.json").read_text())
+    sim = Simulation(desc, host_only=True)
+    types = sim.node_types(layout=N.LAYOUT_REF_TILED if layout_tiled else N.LAYOUT_LEXICOGRAPHIC)
+    sim.close()
+    return types >> 20
+
+
+def reduce_cylinder(d: Path, cfg: dict, out: str):
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
     if cfg["diameter"] != 16:
         raise SystemExit("fixtures are made for the shipped D = 16 case only")
     z_walls = bool(cfg.get("z_walls", False))
@@ -71,13 +119,9 @@ def main(tag: str, out: str):
         halo_val.append(halo[off + pos])
         off += ln
     assert it == cfg["steps"] + 1, (it, cfg)
-    sim = Simulation(desc, host_only=True)
-    types = sim.node_types(layout=N.LAYOUT_REF_TILED)
-    sim.close()
-    cls = types >> 20
+    cls = node_classes(desc)
     rng = np.random.default_rng(20261203)
     if z_walls:
-        from tests.golden.make_golden import tiled_to_lex
         lex = tiled_to_lex(np.arange(n), desc.nx, desc.ny, desc.nz)
         x, y, z = lex % desc.nx, (lex // desc.nx) % desc.ny, lex // (desc.nx * desc.ny)
         b = desc.scan_box
@@ -89,14 +133,76 @@ def main(tag: str, out: str):
     else:
         special = np.flatnonzero(cls != 0)
     idx = np.union1d(special, rng.choice(n, N_RANDOM, replace=False)).astype(np.int64)
-    m64 = m.astype(np.float64)
     np.savez_compressed(
-        out, steps=np.int64(it), idx=idx.astype(np.int32), moments=m[:, idx],
-        field_max=np.abs(m64).max(axis=1), field_sum=m64.sum(axis=1), field_sumsq=(m64 * m64).sum(axis=1),
+        out, steps=np.int64(it), idx=idx.astype(np.int32), moments=m[:, idx], **field_stats(m),
         forces=forces, nxyz=np.array([desc.nx, desc.ny, desc.nz], dtype=np.int32), z_walls=np.int32(z_walls),
         halo_pos=np.stack(halo_pos).astype(np.int64), halo_val=np.stack(halo_val))
     print(f"{out}: {it} steps, {idx.size} sampled nodes, {forces.shape[0]} force rows")
 
 
+def reduce_shedding(d: Path, cfg: dict, out: str):
+    runs = sorted(p for p in d.iterdir() if p.is_dir() and p.name.startswith("run"))
+    forces, times, pressure = [], [], None
+    for rd in runs:
+        forces.append(np.loadtxt(next(rd.rglob("forces.dat")), ndmin=2))
+        times.append(loop_time(rd))
+        if pressure is None:
+            pp = list(rd.rglob("pressure.dat"))
+            if pp:
+                pressure = np.loadtxt(pp[0], skiprows=1, ndmin=2)
+    if not forces:
+        raise SystemExit(f"no runs under {d}")
+    np.savez_compressed(out, forces=np.stack(forces), loop_time=np.stack(times),
+                        pressure=pressure if pressure is not None else np.zeros((0, 3)),
+                        steps=np.int64(cfg["steps"]))
+    print(f"{out}: {len(forces)} runs, {forces[0].shape[0]} force rows each")
+
+
+def reduce_annulus(d: Path, cfg: dict, out: str):
+    from mrlbm_3d_cuda_gb300 import cases
+    desc = cases.reference_annulus(periodic_z=not cfg.get("z_walls", False))
+    nx, ny, nz = desc.nx, desc.ny, desc.nz
+    n = nx * ny * nz
+    it, m, _ = read_restart(next((d / "run").rglob("restart.bin")), n)
+    assert it == cfg["steps"] + 1, (it, cfg)
+    cls = node_classes(desc)
+    lex = tiled_to_lex(np.arange(n), nx, ny, nz)
+    z = lex // (nx * ny)
+    planes = np.isin(z, (0, 1, 2, nz // 2, nz - 3, nz - 2, nz - 1))
+    special = cls != 0
+    rng = np.random.default_rng(20261204)
+    keep = np.flatnonzero(special & planes)
+    rest = np.flatnonzero(special & ~planes)
+    idx = np.union1d(keep, rng.choice(rest, min(20000, rest.size), replace=False))
+    idx = np.union1d(idx, rng.choice(n, N_RANDOM, replace=False)).astype(np.int64)
+    np.savez_compressed(out, steps=np.int64(it), idx=idx.astype(np.int32), moments=m[:, idx], **field_stats(m),
+                        nxyz=np.array([nx, ny, nz], dtype=np.int32), z_walls=np.int32(cfg.get("z_walls", False)),
+                        loop_time=loop_time(d / "run"))
+    print(f"{out}: {it} steps, {idx.size} sampled nodes ({keep.size} wall-region nodes on whole planes)")
+
+
+def reduce_tgv(d: Path, cfg: dict, out: str):
+    nn = int(cfg["n"])
+    n = nn ** 3
+    it, m, _ = read_restart(next((d / "run").rglob("restart.bin")), n)
+    assert it == cfg["steps"] + 1, (it, cfg)
+    rng = np.random.default_rng(20261205)
+    x, z = np.meshgrid(np.arange(nn), np.arange(nn), indexing="ij")
+    plane = lex_to_tiled((x + nn * nn * z).ravel(), nn, nn)  # the whole y = 0 plane
+    idx = np.union1d(rng.choice(n, 60000, replace=False)[:40000], plane).astype(np.int64)
+    np.savez_compressed(out, steps=np.int64(it), idx=idx.astype(np.int32), moments=m[:, idx], **field_stats(m),
+                        nxyz=np.array([nn, nn, nn], dtype=np.int32), loop_time=loop_time(d / "run"),
+                        u0=np.float64(cfg["u0"]), re=np.float64(cfg["re"]))
+    print(f"{out}: {it} steps, {idx.size} sampled nodes, loop {loop_time(d / 'run')}")
+
+
+def main(tag: str, out: str, kind: str | None = None):
+    d = ROOT / "baseline" / "_ref" / tag
+    cfg = json.loads((d / "config.json").read_text())
+    kind = kind or ("shedding" if cfg.get("shipped_run") else cfg.get("case", "cylinder"))
+    {"cylinder": reduce_cylinder, "shedding": reduce_shedding, "annulus": reduce_annulus,
+     "tgv": reduce_tgv}[kind](d, cfg, out)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1], sys.argv[2])
+    main(*sys.argv[1:])

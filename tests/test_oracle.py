@@ -229,7 +229,7 @@ def test_closed_box_at_rest_is_a_fixed_point(built):
     d = N.default_desc(N.GEOM_NONE)
     d.nx, d.ny, d.nz = 16, 16, 8
     d.periodic[0] = d.periodic[1] = d.periodic[2] = 0
-    d.u_max, d.re, d.length, d.omega = 0.0, 10.0, 15.0, 1.2
+    d.u_max, d.re, d.length, d.omega = 0.0, 0.0, 15.0, 1.2  # explicit relaxation rate
     d = N.finalize(d)
     o = oracle.Oracle(d, 64)
     assert len(np.unique(o.node_types() >> 20)) == 27  # bulk + 26 boundary classes
@@ -259,3 +259,22 @@ def test_uniform_stream_through_inlet_and_outlet(built, convective):
     o.close()
     assert np.abs(m[0]).max() < 1e-8 and np.abs(m[1] - 0.05).max() < 1e-8
     assert np.abs(m[2:4]).max() < 1e-14 and np.abs(m[4] - 0.05 ** 2).max() < 1e-8
+
+
+def test_oracle_derives_the_relaxation_rate_itself(built):
+    """The oracle restates the reference's tau chain (cases/cylinder/constants.cuh:52-54,
+    cases/annulus/constants.cuh:73-81) from the physical parameters; the product's descriptor
+    code must give the same float omega for every case builder, so an error in either shows."""
+    import oracle
+    from mrlbm_3d_cuda_gb300 import cases
+    descs = [cases.reference_cylinder(), cases.reference_cylinder(diameter=32), cases.reference_annulus(),
+             cases.c1_cylinder(), cases.c2_taylor_green(), cases.c3_annulus(), cases.c5_turbulent_cylinder(re=400.0),
+             cases.annulus(48, 48, 8, 8.0, 20.0, 0.05, 40.0, u_outer=-0.02)] + cases.c4_batch(8)
+    for d in descs:
+        assert oracle.omega(d) == d.omega, (d.geometry, d.nx, d.re, oracle.omega(d), d.omega)
+    # the reference's own shipped values, written out: cylinder tau = 0.5 + 3 * 0.1 * 16 / 100,
+    # annulus tau = 0.5 + 3 * 0.03 * 32 / 70
+    assert oracle.omega(cases.reference_cylinder()) == np.float32(1.0 / np.float64(np.float32(0.5 + 3 * np.float64(
+        np.float32(np.float32(0.1) * np.float32(16.0)) / np.float32(100.0)))))
+    tgv = oracle.periodic_box_desc(256)
+    assert oracle.omega(tgv) == cases.c2_taylor_green().omega

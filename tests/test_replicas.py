@@ -56,7 +56,7 @@ def test_reference_arm_prints_once_under_torchrun(built):
     port = free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
-           "--gpus", "2", "--steps", "2", "--warmup", "1", "--size", "32", "--ref-slab", "4"]
+           "--gpus", "2", "--steps", "2", "--warmup", "1", "--size", "32", "--ref-budget", "10"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600,
                        env={**os.environ, "OMP_NUM_THREADS": "2"})
     assert r.returncode == 0, r.stderr[-2000:]
@@ -69,7 +69,8 @@ def test_reference_arm_prints_once_under_torchrun(built):
 
 def test_shedding_statistics_of_a_known_signal():
     """bench.shedding_stats on synthetic forces: constant drag plus a sinusoidal lift of known
-    amplitude and frequency gives back Cd, rms Cl and St (the C5 workload's statistics)."""
+    amplitude and frequency gives back Cd, rms Cl and St (the C5 workload's statistics); the
+    zero-crossing frequency also holds for a window that is not a whole number of periods."""
     import math
     import numpy as np
     sys.path.insert(0, str(ROOT))
@@ -86,3 +87,10 @@ def test_shedding_statistics_of_a_known_signal():
     assert abs(cl_rms - 0.3 / math.sqrt(2)) < 1e-9
     assert abs(st - st_true) < 1e-9
     assert all(math.isnan(v) for v in bench.shedding_stats(fx[:3], fy[:3], d, u, nz))
+    from mrlbm_3d_cuda_gb300.statistics import shedding
+    st2 = 0.1835  # the shipped case's shedding: about 9.2 periods in its 8,001-step window
+    t2 = np.arange(48000, 56001)
+    d2, u2, nz2 = 16.0, 0.1, 48
+    q2 = 0.5 * u2 * u2 * d2 * nz2
+    s = shedding(t2, 1.6 * q2 + 0 * t2, 0.28 * q2 * np.sin(2 * math.pi * st2 * u2 / d2 * t2 + 0.7), d2, u2, nz2)
+    assert abs(s.st / st2 - 1) < 1e-4 and s.periods == 8

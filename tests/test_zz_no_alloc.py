@@ -4,18 +4,16 @@ The entry point keeps its scratch in one fixed array of the library's device ima
 every call shares, so this file is collected last: it must pass in a fresh process (first
 use of that array) and after every other test.  Two calls in a row ping-pong between two
 caller-owned device buffers, and each call's output is checked against one mrlbm_step of a
-handle started from the same state, within the 1e-5 field tolerance of the parity tests."""
+handle started from the same state.  The fields must be bit-identical: the entry point runs the
+handle's step kernel, whose results do not depend on the tiling or the work split.  The mass
+and energy sums are FP64 sums of per-thread partials whose grouping follows the work split, so
+they are compared within 1e-9 (mass) and 1e-5 (energy) relative."""
 from __future__ import annotations
 
 import ctypes as C
 
 import numpy as np
 import pytest
-
-from conftest import field_errors
-
-TOL = 1e-5
-
 
 def to_storage(lex: np.ndarray, nx: int, ny: int, nz: int) -> np.ndarray:
     """(10, n) lexicographic moments -> the solver's x-blocked storage layout (flat)."""
@@ -53,7 +51,8 @@ def test_noalloc_rejects_what_it_cannot_hold(built):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("shape,with_diag", [((40, 24, 12), True), ((40, 24, 12), False), ((64, 64, 64), True)])
+@pytest.mark.parametrize("shape,with_diag", [((40, 24, 12), True), ((40, 24, 12), False), ((64, 64, 64), True),
+                                             ((32, 16, 4096), False)])
 def test_noalloc_step_matches_handle_step(cuda_device, shape, with_diag):
     import torch
     from mrlbm_3d_cuda_gb300 import Simulation, cases
@@ -84,8 +83,7 @@ def test_noalloc_step_matches_handle_step(cuda_device, shape, with_diag):
         want = sim.moments()
         got = from_storage(dst.cpu().numpy(), nx, ny, nz)
         assert np.isfinite(got).all()
-        err = field_errors(got, want, u0)[:, 0]
-        assert err.max() < TOL, (call, np.array2string(err, precision=3))
+        assert np.array_equal(got, want.reshape(10, -1)), (call, np.abs(got - want.reshape(10, -1)).max(axis=1))
         if with_diag:
             _, vals = sim.diagnostics()
             assert abs(diag[0] - vals[-1, 0]) <= 1e-9 * abs(vals[-1, 0]), (call, diag[0], vals[-1])
