@@ -155,6 +155,14 @@ def cpu_baseline(n: int, steps: int, bits: int = 64, budget_s: float = 20.0):
                       f"FP{bits} restatement of the reference step, OpenMP {cores} threads"}
 
 
+# The reference's own GPU build on the same workload and GPU model (stock time loop timed with
+# CUDA events in a staged copy of its sources): recorded in profiles/reference_build_loops.md.
+_REF_SRC = {"kind": "reference build, stock loop", "source": "profiles/reference_build_loops.md"}
+REFERENCE_GPU = {"tgv256": {"value": 9451.0, "unit": "MLUPS", "ms_per_step": 1.7752, "steps": 196, **_REF_SRC},
+                 "cylinder16": {"value": 6872.0, "unit": "MLUPS", "ms_per_step": 0.33797, "steps": 55996, **_REF_SRC},
+                 "annulus": {"value": 7173.0, "unit": "MLUPS", "ms_per_step": 0.6601, "steps": 996, **_REF_SRC}}
+
+
 def watchdog_steps(first: int, k: int, every: int = 64) -> int:
     """Steps it in [first, first + k) on which the divergence watchdog runs ((it + 1) % every == 0)."""
     return (first + k) // every - first // every
@@ -429,12 +437,20 @@ def run_ours(args):
     from mrlbm_3d_cuda_gb300 import native as N
 
     storage = args.storage
-    cyl = args.workload == "cylinder"
-    if cyl:
+    cyl = args.workload in ("cylinder", "annulus")  # cases with walls: reference initial state
+    ref_gpu = None
+    if args.workload == "cylinder":
         desc = cases.reference_cylinder(STORAGE[storage], args.diameter)
         workload = (f"reference cylinder case scaled to D={args.diameter}: {desc.nx}x{desc.ny}x{desc.nz} D3Q27, "
                     f"Re=100, U=0.1, convective outlet, periodic y/z, {storage} moment storage")
         metric = f"MLUPS (D3Q27 MR-LBM, cylinder D={args.diameter} {desc.nx}x{desc.ny}x{desc.nz})"
+        ref_gpu = REFERENCE_GPU["cylinder16"] if args.diameter == 16 else None
+    elif args.workload == "annulus":
+        desc = cases.reference_annulus(STORAGE[storage])
+        workload = (f"reference annulus case: {desc.nx}x{desc.ny}x{desc.nz} D3Q27, r = 32 / 64, inner wall 0.03, "
+                    f"Re=70, periodic z, {storage} moment storage")
+        metric = f"MLUPS (D3Q27 MR-LBM, annulus {desc.nx}x{desc.ny}x{desc.nz})"
+        ref_gpu = REFERENCE_GPU["annulus"]
     else:
         desc = cases.c2_taylor_green(args.n, STORAGE[storage])
         workload = f"taylor-green {args.n}^3 D3Q27, u0=0.05, Re=1600, {storage} moment storage"
@@ -523,6 +539,10 @@ def run_ours(args):
         line["storage_comparison"]["f32"]["value"] = value
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.n, args.cpu_steps, bits=64)
+    if not cyl and args.n == 256:
+        ref_gpu = REFERENCE_GPU["tgv256"]
+    if ref_gpu:
+        line["reference_gpu"] = dict(ref_gpu, speedup=value / world / ref_gpu["value"])
     sim.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -540,7 +560,7 @@ def main():
     ap.add_argument("--stochastic-rounding", action="store_true",
                     help="16-bit storage: round the time-step stores stochastically (cvt.rs)")
     ap.add_argument("--size", dest="n", type=int, default=256, help="TGV grid edge (n^3)")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder", "batch", "c5"])
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder", "annulus", "batch", "c5"])
     ap.add_argument("--batch-cases", type=int, default=64)
     ap.add_argument("--re", type=float, default=3900.0, help="Reynolds number of the c5 workload")
     ap.add_argument("--c5-init", default="noisy", choices=["noisy", "rest"])

@@ -3,8 +3,8 @@ sources, where they lie, into oracle/_ref/ — test infrastructure only.
 
 * ``ref_geometry``: a host-only program (no GPU) that runs the reference's own node
   classification for its shipped cylinder case and dumps the result (see
-  ref_harness/ref_geometry.cu).  Built when the reference tree is present (this
-  container); the GPU machine has no reference tree and uses nothing from here.
+  ref_harness/ref_geometry.cu).  Built when MRLBM_REFERENCE names the reference checkout
+  (the directory that holds MRLBM_3D/); where it is unset nothing here is built or used.
 * ``ref_geometry_annulus``: the annulus case's classification for both walls
   (ref_harness/ref_geometry_annulus.cu).  The reference selects the case at compile time
   (``#define CASE_ID`` in config.h:8), and its annulus case does not compile as shipped:
@@ -34,12 +34,18 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REF_ROOT = Path(os.environ.get("MRLBM_REFERENCE", "/root/reference"))
-REF_SRC = REF_ROOT / "MRLBM_3D" / "src"
+
+
+def _ref_src() -> Path | None:
+    """The reference's MRLBM_3D/src, from the MRLBM_REFERENCE environment variable (the
+    directory holding MRLBM_3D/); None when it is unset."""
+    loc = os.environ.get("MRLBM_REFERENCE")
+    return Path(loc) / "MRLBM_3D" / "src" if loc else None
 
 
 def reference_present() -> bool:
-    return (REF_SRC / "main.cu").exists()
+    src = _ref_src()
+    return src is not None and (src / "main.cu").exists()
 
 
 def _nvcc() -> str:
@@ -59,7 +65,7 @@ def build_ref_geometry(force: bool = False) -> Path | None:
         return exe
     OUT.mkdir(exist_ok=True)
     cmd = [_nvcc(), "-std=c++17", "-O2", "-x", "cu", "-gencode", "arch=compute_103a,code=sm_103a",
-           "-I", str(REF_SRC), "-I", str(REF_SRC.parent), '-DID_SIM="000"', "-w", str(src), "-o", str(exe)]
+           "-I", str(_ref_src()), "-I", str(_ref_src().parent), '-DID_SIM="000"', "-w", str(src), "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"reference geometry harness failed to build:\n{' '.join(cmd)}\n{r.stderr}")
@@ -76,7 +82,7 @@ def build_ref_geometry_zwall(force: bool = False) -> Path | None:
     OUT.mkdir(exist_ok=True)
     with tempfile.TemporaryDirectory() as td:
         tree = Path(td) / "src"
-        shutil.copytree(REF_SRC, tree, ignore=shutil.ignore_patterns("*.o"))
+        shutil.copytree(_ref_src(), tree, ignore=shutil.ignore_patterns("*.o"))
         consts = tree / "cases" / "cylinder" / "constants.cuh"
         lines = consts.read_text().split("\n")
         hits = [i for i, ln in enumerate(lines) if ln.strip().startswith("#define Z_PERIODIC 1")]
@@ -85,7 +91,7 @@ def build_ref_geometry_zwall(force: bool = False) -> Path | None:
         lines[hits[0]] = "#define Z_PERIODIC 0"
         consts.write_text("\n".join(lines))
         cmd = [_nvcc(), "-std=c++17", "-O2", "-x", "cu", "-gencode", "arch=compute_103a,code=sm_103a",
-               "-I", str(tree), "-I", str(REF_SRC.parent), '-DID_SIM="000"', "-w", str(src), "-o", str(exe)]
+               "-I", str(tree), "-I", str(_ref_src().parent), '-DID_SIM="000"', "-w", str(src), "-o", str(exe)]
         r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"reference z-wall geometry harness failed to build:\n{' '.join(cmd)}\n{r.stderr}")
@@ -104,7 +110,7 @@ def _staged_build(name: str, harness: str, edits, force: bool) -> Path | None:
     OUT.mkdir(exist_ok=True)
     with tempfile.TemporaryDirectory() as td:
         tree = Path(td) / "src"
-        shutil.copytree(REF_SRC, tree, ignore=shutil.ignore_patterns("*.o"))
+        shutil.copytree(_ref_src(), tree, ignore=shutil.ignore_patterns("*.o"))
         for rel, old, new in edits:
             f = tree / rel
             lines = f.read_text().split("\n")
@@ -117,7 +123,7 @@ def _staged_build(name: str, harness: str, edits, force: bool) -> Path | None:
                 lines[hits[0]] = new
             f.write_text("\n".join(lines))
         cmd = [_nvcc(), "-std=c++17", "-O2", "-x", "cu", "-gencode", "arch=compute_103a,code=sm_103a",
-               "-I", str(tree), "-I", str(REF_SRC.parent), '-DID_SIM="000"', "-w", str(src), "-o", str(exe)]
+               "-I", str(tree), "-I", str(_ref_src().parent), '-DID_SIM="000"', "-w", str(src), "-o", str(exe)]
         r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"reference harness {name} failed to build:\n{' '.join(cmd)}\n{r.stderr}")

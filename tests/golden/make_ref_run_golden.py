@@ -33,6 +33,8 @@ Kinds (the staged case, from baseline/_ref/<tag>/config.json):
 
 Run on the GPU machine from the repository root (after oracle/ref_gpu.py build/run):
     python tests/golden/make_ref_run_golden.py <tag> <out.npz>
+then, for the annulus and Taylor-Green fixtures, add the oracle's FP32 rounding floor (e32):
+    python tests/golden/make_ref_run_golden.py e32 <fixture.npz> annulus|tgv
 """
 from __future__ import annotations
 
@@ -196,7 +198,44 @@ def reduce_tgv(d: Path, cfg: dict, out: str):
     print(f"{out}: {it} steps, {idx.size} sampled nodes, loop {loop_time(d / 'run')}")
 
 
+def add_e32(path: str, kind: str):
+    """Add the FP32 rounding floor of the reference algorithm to a fixture: the distance of the
+    FP32 oracle from the FP64 oracle after the fixture's step count, on its sampled nodes
+    (per field: scaled max, plain max and L2 relative, as tests/conftest.field_errors), and the
+    FP32 oracle's own distance from the reference build.  Run where the oracle is built (the
+    annulus at 1,001 steps takes a few minutes on 16 cores)."""
+    import oracle
+    from mrlbm_3d_cuda_gb300 import cases
+    sys.path.insert(0, str(ROOT / "tests"))
+    from conftest import field_errors
+    g = dict(np.load(path))
+    steps, idx = int(g["steps"]), g["idx"].astype(np.int64)
+    nx, ny, nz = (int(v) for v in g["nxyz"])
+    if kind == "annulus":
+        desc, init, params, u_ref = cases.reference_annulus(), 0, (), 0.03  # INIT_REFERENCE_NOISE
+    elif kind == "tgv":
+        desc, init, params, u_ref = oracle.periodic_box_desc(nx, 0.05, 1600.0), 2, (
+            float(np.float32(0.05)), nx / (2 * np.pi)), 0.05
+    else:
+        desc, init, params, u_ref = cases.reference_cylinder(), 0, (), 0.1
+    lex = tiled_to_lex(idx, nx, ny, nz)
+    got = {}
+    for bits in (32, 64):
+        o = oracle.Oracle(desc, bits)
+        o.init(init, params)
+        o.step(steps)
+        got[bits] = o.moments().reshape(10, -1)[:, lex]
+        o.close()
+    e = field_errors(got[32], got[64], u_ref)
+    g["e32"], g["e32_plain"], g["e32_l2"] = e[:, 0], e[:, 1], e[:, 2]
+    g["o32_vs_ref"] = field_errors(got[32], g["moments"], u_ref)
+    np.savez_compressed(path, **g)
+    print(f"{path}: e32 {np.array2string(e[:, 0], precision=2)}", flush=True)
+
+
 def main(tag: str, out: str, kind: str | None = None):
+    if tag == "e32":  # add the FP32 rounding floor to an existing fixture: e32 <fixture> <kind>
+        return add_e32(out, kind)
     d = ROOT / "baseline" / "_ref" / tag
     cfg = json.loads((d / "config.json").read_text())
     kind = kind or ("shedding" if cfg.get("shipped_run") else cfg.get("case", "cylinder"))

@@ -80,3 +80,48 @@ def test_largest_single_gpu_grid_shift_invariance(cuda_device):
     assert same, "the step does not commute with a periodic shift"
     assert np.isfinite(diag).all()
     assert abs(diag[-1, 0] - diag[0, 0]) / (1024 * 512 * 256) < 1e-6 * steps
+
+
+C2_STORAGE = {"f32": (0, 0), "f16": (1, 0), "f16sr": (1, 1), "bf16": (2, 0), "bf16sr": (2, 1)}
+# max over t of |E/E64 - 1| and of |eps - eps64| / max eps64 (eps = -dE/dt over 50 steps)
+C2_BOUND = {"f32": (1e-5, 1e-3), "f16": (5e-2, 1.0), "f16sr": (2e-3, 5e-2), "bf16": (0.3, 3.0),
+            "bf16sr": (2e-2, 0.3)}
+
+
+@pytest.mark.parametrize("storage", list(C2_STORAGE))
+def test_c2_energy_and_dissipation_against_fp64(cuda_device, storage):
+    """C2 as configured: Taylor-Green 256^3, u0 = 0.05, Re = 1600, 5000 steps, E(t) =
+    sum |u|^2 / 2 and its decay rate eps(t) every 50 steps against the FP64 oracle run of the
+    same field (tests/golden/tgv256_fp64_energy.npz, made by make_tgv_energy_golden.py)."""
+    from conftest import GOLDEN, _PARITY_LOG
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    path = GOLDEN / "tgv256_fp64_energy.npz"
+    if not path.exists():
+        pytest.skip("FP64 energy fixture not generated")
+    g = np.load(path)
+    steps, e64 = g["steps"], g["energy"]
+    every = int(steps[1] - steps[0])
+    st, sr = C2_STORAGE[storage]
+    desc = cases.c2_taylor_green(256, st)
+    desc.stochastic_rounding = sr
+    sim = Simulation(desc, init=False)
+    sim.init(N.INIT_TAYLOR_GREEN, cases.tgv_params(desc))
+    m0 = sim.moments().reshape(10, -1).astype(np.float64)
+    e = [0.5 * float((m0[1] ** 2 + m0[2] ** 2 + m0[3] ** 2).sum())]
+    del m0
+    for _ in steps[1:]:
+        sim.set_sampling(0, 0)
+        sim.step(every - 1)
+        sim.set_sampling(0, 1)
+        sim.step(1)  # its sample is the state after these steps
+    sim.sync()
+    _, diag = sim.diagnostics()
+    sim.close()
+    e = np.array(e + list(diag[-(len(steps) - 1):, 1]))
+    eps, eps64 = -np.diff(e) / every, -np.diff(e64) / every
+    e_err = float(np.abs(e / e64 - 1).max())
+    eps_err = float((np.abs(eps - eps64) / np.abs(eps64).max()).max())
+    _PARITY_LOG[f"c2_energy_{storage}"] = {"max_rel_E": e_err, "max_rel_eps": eps_err,
+                                           "E_end_rel": float(e[-1] / e64[-1] - 1)}
+    assert e_err < C2_BOUND[storage][0] and eps_err < C2_BOUND[storage][1], (storage, e_err, eps_err)

@@ -196,6 +196,28 @@ def test_fp32_oracle_matches_reference_build(built, fixture):
     o.close()
 
 
+def test_fp32_oracle_matches_reference_build_annulus(built):
+    """The oracle pinned against the reference's own build of its shipped annulus (136 x 136 x
+    256, inner wall moving at 0.03 in the rotated frame, outer wall fixed, Re 70): 11 steps
+    from the reference's initial state.  This pins the moving-wall closure and the outer
+    wall's inward probe of the restatement against the reference itself, not only against an
+    analytic profile.  Fields within max(1e-5, 2 e32) at the fixture's nodes, e32 being the
+    FP32 oracle's distance from the FP64 oracle stored in the fixture."""
+    import oracle
+    from conftest import GOLDEN, field_errors
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    from tests.golden.make_golden import tiled_to_lex
+    g = np.load(GOLDEN / "ref_annulus_run_n10.npz")
+    o = oracle.Oracle(cases.reference_annulus(), 32)
+    o.init(N.INIT_REFERENCE_NOISE)
+    o.step(int(g["steps"]))
+    m = o.moments().reshape(10, -1)[:, tiled_to_lex(g["idx"], *g["nxyz"])]
+    o.close()
+    err = field_errors(m, g["moments"], 0.03)[:, 0]
+    assert (err <= np.maximum(1e-5, 2.0 * g["e32"])).all(), np.array2string(err, precision=3)
+
+
 def test_annulus_couette_profile(built):
     """Sub-critical Taylor-Couette flow (Re 1.2 on the gap, inner wall moving, outer at rest)
     reaches the analytic profile u_theta = A r + B / r with u(r_i) = U_i and u(r_o) = 0: the

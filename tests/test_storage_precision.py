@@ -19,6 +19,8 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
+from conftest import field_errors, record_parity
+
 pytestmark = pytest.mark.gpu
 STORAGE = {"f32": (0, 0), "f16": (1, 0), "bf16": (2, 0), "f16sr": (1, 1), "bf16sr": (2, 1)}
 
@@ -83,8 +85,9 @@ def cylinder_oracle(cuda_device):
     for _ in range(500):
         o.step(1, forces=True)
         fx.append(o.forces()[0, 0])
+    m = o.moments()
     o.close()
-    return np.array(fx)
+    return np.array(fx), m
 
 
 @pytest.mark.parametrize("storage,tol", [("f32", 1e-4), ("f16", 5e-3), ("bf16", 1.5e-2), ("f16sr", 2e-4),
@@ -102,7 +105,7 @@ def test_cylinder_drag_within_half_percent(cylinder_oracle, storage, tol):
     sim.step(2000)
     _, f = sim.force_history()
     sim.close()
-    cd, cd64 = f[-500:, 0, 0].mean(), cylinder_oracle.mean()
+    cd, cd64 = f[-500:, 0, 0].mean(), cylinder_oracle[0].mean()
     assert abs(cd / cd64 - 1) < tol, (storage, cd, cd64)
 
 
@@ -169,3 +172,45 @@ def test_stochastic_rounding_is_reproducible(cuda_device, storage, tmp_path, mon
     sim.step(20)
     assert not np.array_equal(base, sim.moments())  # the rounding mode is in effect
     sim.close()
+
+
+@pytest.fixture(scope="module")
+def tgv_oracle_fields(cuda_device):
+    import oracle
+    from mrlbm_3d_cuda_gb300 import cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    desc = cases.periodic_box(64, u0=0.05, re=1600.0)
+    o = oracle.Oracle(desc, 64)
+    o.init(N.INIT_TAYLOR_GREEN, cases.tgv_params(desc))
+    o.step(1000)
+    m = o.moments()
+    o.close()
+    return m
+
+
+# Per-field error bounds against the FP64 oracle (scaled metric of conftest.field_errors:
+# max |a - b| / max(||b||inf, s_f), s_f = 1 for rho, U for u, cs2 for m).
+FIELD_BOUND = {"f32": 2e-5, "f16": 5e-2, "f16sr": 5e-2, "bf16": 0.5, "bf16sr": 0.5}
+
+
+@pytest.mark.parametrize("storage", list(STORAGE))
+def test_per_field_error_against_fp64(tgv_oracle_fields, cylinder_oracle, storage):
+    """Every moment field of each storage mode against the FP64 oracle run: Taylor-Green 64^3
+    (Re 1600, 1000 steps) and the C1 cylinder (128 x 64 x 32, Re 100, 2000 steps from rest).
+    The per-field max / plain / L2 errors go to the parity report; the scaled max is bounded."""
+    from mrlbm_3d_cuda_gb300 import Simulation, cases
+    from mrlbm_3d_cuda_gb300 import native as N
+    runs = [("tgv64_1000", make(cases.periodic_box, storage, 64, u0=0.05, re=1600.0), tgv_oracle_fields, 1000,
+             N.INIT_TAYLOR_GREEN, True),
+            ("c1_2000", make(cases.c1_cylinder, storage), cylinder_oracle[1], 2000, N.INIT_REST, False)]
+    worst = 0.0
+    for name, desc, want, steps, kind, tgv in runs:
+        sim = Simulation(desc, init=False)
+        sim.init(kind, cases.tgv_params(desc) if tgv else ())
+        sim.step(steps)
+        got = sim.moments()
+        sim.close()
+        errs = field_errors(got, want, 0.05)
+        record_parity(f"storage_{storage}_{name}_vs_fp64", errs)
+        worst = max(worst, float(errs[:, 0].max()))
+    assert worst < FIELD_BOUND[storage], (storage, worst)
