@@ -56,6 +56,7 @@ extern "C" {
 #define MRLBM_STORAGE_F32 0  /* moments stored as float                                   */
 #define MRLBM_STORAGE_F16 1  /* moments stored as IEEE half, scaled deviations            */
 #define MRLBM_STORAGE_BF16 2 /* moments stored as bfloat16, scaled deviations             */
+#define MRLBM_STORAGE_F16_U32 3 /* velocity in FP32, rho - rho0 and m as FP16 scaled deviations */
 
 #define MRLBM_MASS_EQUILIBRIUM 0 /* MassBC::Equilibrium (common/types.cuh:14-19)           */
 #define MRLBM_MASS_STRONG 1      /* MassBC::Strong                                         */

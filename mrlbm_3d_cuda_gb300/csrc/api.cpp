@@ -140,6 +140,11 @@ void default_tiling(int &ty, int &lz) {
 
 int setup_tiling(mrlbm_handle *h, int ty, int lz);
 
+// Bytes of one storage element: FP32 and the hybrid mode's words 4, FP16 / BF16 halves 2.
+int storage_element_bytes(int storage) {
+    return storage == MRLBM_STORAGE_F16 || storage == MRLBM_STORAGE_BF16 ? 2 : 4;
+}
+
 // (Re)build everything that depends on the step kernel's tiling: tile slots and side buffer,
 // the non-bulk node list, work items, grid size and the device StepArgs.  Node words and
 // geometry do not depend on it, so the autotuner can switch tilings cheaply.
@@ -515,7 +520,7 @@ int mrlbm_case_desc_finalize(mrlbm_case_desc *d) {
     if (d->nx < 8 || d->ny < 8 || d->nz < 4) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "grid too small");
     if ((int64_t)d->nx * d->ny * d->nz >= (1LL << 31) * 8)
         return fail(nullptr, MRLBM_ERR_INVALID_ARG, "grid too large");
-    if (d->storage < 0 || d->storage > 2) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "bad storage");
+    if (d->storage < 0 || d->storage > 3) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "bad storage");
     if (d->geometry < 0 || d->geometry > 2) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "bad geometry");
     if (!(d->rho0 > 0.f)) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "rho0 must be positive");
     if (d->omega <= 0.f && !(d->re > 0.f)) return fail(nullptr, MRLBM_ERR_INVALID_ARG, "need re > 0 or omega > 0");
@@ -559,7 +564,7 @@ int mrlbm_create_host(const mrlbm_case_desc *din, mrlbm_handle **out) {
     if (!ge.empty()) return fail(nullptr, MRLBM_ERR_INVALID_ARG, ge);
     h->n = (int64_t)d.nx * d.ny * d.nz;
     h->storage = d.storage;
-    h->vbytes = d.storage == MRLBM_STORAGE_F32 ? 4 : 2;
+    h->vbytes = storage_element_bytes(d.storage);
     h->host_only = true;
     *out = h.release();
     return MRLBM_OK;
@@ -598,12 +603,13 @@ int mrlbm_create(const mrlbm_case_desc *din, mrlbm_handle **out) {
     }
     const Geometry &g = h->geo;
     h->n = (int64_t)d.nx * d.ny * d.nz;
-    h->fs = aos_elements(d.nx, d.ny, d.nz);  // storage elements per moment buffer
+    // storage elements per moment buffer (the hybrid mode keeps 7 words per node)
+    h->fs = aos_elements(d.nx, d.ny, d.nz, d.storage == MRLBM_STORAGE_F16_U32 ? 7 : 10);
     h->storage = d.storage;
-    h->vbytes = d.storage == MRLBM_STORAGE_F32 ? 4 : 2;
+    h->vbytes = storage_element_bytes(d.storage);
     for (int k = 0; k < 3; ++k) {
         float s = d.storage_scale[k];
-        if (d.storage == MRLBM_STORAGE_F32) s = 1.f;
+        if (d.storage == MRLBM_STORAGE_F32 || (d.storage == MRLBM_STORAGE_F16_U32 && k == 1)) s = 1.f;  // FP32 values
         else if (!(s > 0.f)) {
             const float u = d.u_max > 0.f ? d.u_max : 0.05f;
             s = k == 1 ? 1.0f / u : 1.0f / (u * u);

@@ -13,16 +13,36 @@ namespace mrlbm {
 // keeps one field per 32-node line; 2-byte storage keeps the field pairs (2j, 2j+1) of a node
 // in one 32-bit word, so a lane moves two fields per access.  aos_index is the element of a
 // node's field 0, field_offset the distance of field k from it.
+// The hybrid storage mode (FP32 velocity, FP16 density deviation and second moments) keeps
+// 7 words per node: ux, uy, uz as FP32, then the FP16 pairs (rho - rho0, mxx), (myy, mzz),
+// (mxy, mxz), (myz, unused).  HybridWord is its 32-bit storage element.
 constexpr int kXBlock = 32;
-inline __host__ __device__ int64_t aos_index(int x, int y, int z, int nxb, int ny, int esz) {
-    const int64_t run = ((((int64_t)z * ny + y) * nxb + (x >> 5)) * 10) * kXBlock;
+struct HybridWord {
+    uint32_t bits;
+};
+template <typename S>
+struct StorageLayout {
+    static constexpr int esz = (int)sizeof(S);  // bytes per storage element
+    static constexpr int per_node = 10;         // elements per node (32-node run: per_node x 32)
+};
+template <>
+struct StorageLayout<HybridWord> {
+    static constexpr int esz = 4;
+    static constexpr int per_node = 7;
+};
+inline __host__ __device__ int64_t aos_index(int x, int y, int z, int nxb, int ny, int esz, int per_node = 10) {
+    const int64_t run = ((((int64_t)z * ny + y) * nxb + (x >> 5)) * per_node) * kXBlock;
     return run + (esz == 4 ? (x & (kXBlock - 1)) : 2 * (x & (kXBlock - 1)));
+}
+template <typename S>
+inline __host__ __device__ int64_t aos_at(int x, int y, int z, int nxb, int ny) {
+    return aos_index(x, y, z, nxb, ny, StorageLayout<S>::esz, StorageLayout<S>::per_node);
 }
 inline __host__ __device__ constexpr int field_offset(int k, int esz) {
     return esz == 4 ? k * kXBlock : (k >> 1) * (2 * kXBlock) + (k & 1);
 }
-inline __host__ __device__ int64_t aos_elements(int nx, int ny, int nz) {
-    return (int64_t)nz * ny * ((nx + kXBlock - 1) / kXBlock) * 10 * kXBlock;
+inline __host__ __device__ int64_t aos_elements(int nx, int ny, int nz, int per_node = 10) {
+    return (int64_t)nz * ny * ((nx + kXBlock - 1) / kXBlock) * per_node * kXBlock;
 }
 
 // Low-precision storage keeps scaled deviations from the rest state: stored = value * scale,

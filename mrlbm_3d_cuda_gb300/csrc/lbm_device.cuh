@@ -126,7 +126,7 @@ __device__ __forceinline__ void evaluate(const float f[27], Mom &m) {
     const float sxy = (e7 - e13) + ((e19 + e21) - (e23 + e25));
     const float sxz = (e9 - e15) + ((e19 - e21) + (e23 - e25));
     const float syz = (e11 - e17) + ((e19 - e21) - (e23 - e25));
-    const float inv = 1.0f / rho;
+    const float inv = __frcp_rn(rho);  // correctly rounded, as 1.0f / rho
     m.rho = rho;
     m.ux = jx * inv;
     m.uy = jy * inv;

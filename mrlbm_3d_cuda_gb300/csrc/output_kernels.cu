@@ -50,7 +50,7 @@ __global__ void halo_export_kernel(const StepArgs *__restrict__ ga, int parity, 
     const int64_t gx = a.nx / kBX, gy = a.ny / kBY;
     const int64_t block = x / kBX + gx * (y / kBY + gy * (z / kBZ));
     float raw[10], f[27];
-    load_raw<S>((const S *)a.m[parity], aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S)), raw);
+    load_raw<S>((const S *)a.m[parity], aos_at<S>(x, y, z, a.nxb, a.ny), raw);
     rebuild<S>(raw, a.rho0, a.sc, f);
 #pragma unroll
     for (int j = 0; j < kQF; ++j) {
@@ -69,7 +69,7 @@ __global__ void halo_export_kernel(const StepArgs *__restrict__ ga, int parity, 
 // Density deviation at (x, y, z) of the stored moments.
 template <typename S>
 __device__ __forceinline__ float rho_dev(const StepArgs &a, const S *m, int x, int y, int z) {
-    const float v = to_f<S>(m[aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S))]);
+    const float v = load_field<S>(m, aos_at<S>(x, y, z, a.nxb, a.ny), 0);
     return std::is_same<S, float>::value ? v : v * a.sc.is[0];
 }
 
@@ -183,6 +183,10 @@ cudaError_t launch_halo_export(const StepArgs *ga, int parity, int storage, int6
             halo_export_kernel<__nv_bfloat16><<<blocks, 256, 0, s>>>(ga, parity, faces[0], faces[1], faces[2],
                                                                      faces[3], faces[4], faces[5]);
             break;
+        case MRLBM_STORAGE_F16_U32:
+            halo_export_kernel<HybridWord><<<blocks, 256, 0, s>>>(ga, parity, faces[0], faces[1], faces[2],
+                                                                     faces[3], faces[4], faces[5]);
+            break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -198,6 +202,9 @@ cudaError_t launch_inlet_density(const StepArgs *ga, int buf, int storage, doubl
         case MRLBM_STORAGE_BF16:
             inlet_density_kernel<__nv_bfloat16><<<1, kInletThreads, 0, s>>>(ga, buf, state, slot, n_avg);
             break;
+        case MRLBM_STORAGE_F16_U32:
+            inlet_density_kernel<HybridWord><<<1, kInletThreads, 0, s>>>(ga, buf, state, slot, n_avg);
+            break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -212,6 +219,9 @@ cudaError_t launch_surface_pressure(const StepArgs *ga, int buf, int storage, in
         case MRLBM_STORAGE_F16: surface_pressure_kernel<__half><<<blocks, 128, 0, s>>>(ga, buf, wall, avg, n_avg); break;
         case MRLBM_STORAGE_BF16:
             surface_pressure_kernel<__nv_bfloat16><<<blocks, 128, 0, s>>>(ga, buf, wall, avg, n_avg);
+            break;
+        case MRLBM_STORAGE_F16_U32:
+            surface_pressure_kernel<HybridWord><<<blocks, 128, 0, s>>>(ga, buf, wall, avg, n_avg);
             break;
         default: return cudaErrorInvalidValue;
     }

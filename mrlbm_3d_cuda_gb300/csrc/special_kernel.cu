@@ -53,7 +53,7 @@ __device__ __noinline__ Mom pulled_rho_u(const StepArgs &a, const S *__restrict_
     for (int q = 0; q < 27; ++q) {
         const int xs = (x - cxq(q) + a.nx) % a.nx, ys = (y - cyq(q) + a.ny) % a.ny, zs = (z - czq(q) + a.nz) % a.nz;
         float raw[10], g[27];
-        load_raw<S>(src, aos_index(xs, ys, zs, a.nxb, a.ny, (int)sizeof(S)), raw);
+        load_raw<S>(src, aos_at<S>(xs, ys, zs, a.nxb, a.ny), raw);
         rebuild<S>(raw, a.rho0, a.sc, g);
         f[q] = g[q];
     }
@@ -73,7 +73,7 @@ __device__ __forceinline__ int special_node(const StepArgs &a, int parity, bool 
     if (cls == C_BULK) {
         evaluate(fl, m);
     } else {
-        const Mom prev = load_mom<S>(src, aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S)), a.rho0, a.sc);
+        const Mom prev = load_mom<S>(src, aos_at<S>(x, y, z, a.nxb, a.ny), a.rho0, a.sc);
         m = prev;  // nodes without a closure keep their pre-stream moments
         if (cls == C_SOLID) {
             fluid = false;
@@ -106,7 +106,7 @@ __device__ __forceinline__ int special_node(const StepArgs &a, int parity, bool 
                     c.west_prev = pulled_rho_u<S>(a, src, x - 1, y, z);
                     c.self_prev = rho_u_of(fl);
                 } else {
-                    c.west_prev = load_mom<S>(src, aos_index(x - 1, y, z, a.nxb, a.ny, (int)sizeof(S)), a.rho0, a.sc);
+                    c.west_prev = load_mom<S>(src, aos_at<S>(x - 1, y, z, a.nxb, a.ny), a.rho0, a.sc);
                 }
             }
             Mom o = prev;
@@ -173,8 +173,8 @@ __global__ void __launch_bounds__(kListThreads)
         Mom m;
         const int code = special_node<S>(a, parity, force != 0, w, f, x, y, z, slot, tx * TILE_X, ty * a.tile_y, m);
         if (code) {
-            const int64_t ai = aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S));
-            if (sizeof(S) == 2 && a.sr_step)
+            const int64_t ai = aos_at<S>(x, y, z, a.nxb, a.ny);
+            if (kScaled<S> && a.sr_step)
                 store_mom_sr<S>(dst, ai, m, a.rho0, a.sc, sr_key(sr_step_seed(*a.sr_step), x, y, z, a.nx, a.ny));
             else
                 store_mom<S>(dst, ai, m, a.rho0, a.sc);
@@ -229,6 +229,10 @@ cudaError_t launch_special_list(const StepLaunch &l, int storage, int n_blocks, 
             special_list_kernel<__nv_bfloat16, false>
                 <<<n_blocks, kListThreads, 0, s>>>(l.ga, nullptr, l.parity, f, diag_part);
             break;
+        case MRLBM_STORAGE_F16_U32:
+            special_list_kernel<HybridWord, false>
+                <<<n_blocks, kListThreads, 0, s>>>(l.ga, nullptr, l.parity, f, diag_part);
+            break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -246,6 +250,10 @@ cudaError_t launch_special_list_batch(const BatchArgs *ba, int parity, int force
             break;
         case MRLBM_STORAGE_BF16:
             special_list_kernel<__nv_bfloat16, true>
+                <<<n_blocks, kListThreads, 0, s>>>(nullptr, ba, parity, force, nullptr);
+            break;
+        case MRLBM_STORAGE_F16_U32:
+            special_list_kernel<HybridWord, true>
                 <<<n_blocks, kListThreads, 0, s>>>(nullptr, ba, parity, force, nullptr);
             break;
         default: return cudaErrorInvalidValue;

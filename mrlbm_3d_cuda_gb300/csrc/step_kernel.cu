@@ -134,7 +134,7 @@ __device__ __forceinline__ void gather_evaluate(const float *up, const float *fl
                                    MRLBM_P(15), MRLBM_P(21));
 #undef MRLBM_P
     const float rho = (u.s0 + c.s0) + d.s0;
-    const float inv = 1.0f / rho;
+    const float inv = __frcp_rn(rho);  // correctly rounded, as 1.0f / rho
     const float iu = SCALED ? __fmul_rn(inv, su) : inv, im = SCALED ? __fmul_rn(inv, sm) : inv;
     const float cs = SCALED ? __fmul_rn(-kCs2, sm) : -kCs2;
     m.rho = rho;
@@ -258,8 +258,8 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         rho0 = c->rho0;
         sc = c->sc;
         plane = (int64_t)nx * ny;
-        zst = (int64_t)ny * nxb * 10 * kXBlock;
-        if constexpr (sizeof(S) == 2) {
+        zst = (int64_t)ny * nxb * StorageLayout<S>::per_node * kXBlock;
+        if constexpr (kScaled<S>) {
             sr_on = c->sr_step != nullptr;
             sr_seed = sr_on ? sr_step_seed(*c->sr_step) : 0u;
             omega_u = c->omega * (c->sc.s[2] * (c->sc.is[1] * c->sc.is[1]));
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         int64_t cxy = 0;
         bool active = own;
         if (own) {
-            cxy = aos_index(x, y, 0, nxb, ny, (int)sizeof(S));
+            cxy = aos_at<S>(x, y, 0, nxb, ny);
         } else if (!owner) {
             int rx, ry, sd;
             const int r = tid - G::NOWN;
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 int gx = x0 + rx, gy = y0 + ry;
                 gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
                 gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
-                cxy = aos_index(gx, gy, 0, nxb, ny, (int)sizeof(S));
+                cxy = aos_at<S>(gx, gy, 0, nxb, ny);
                 active = true;
             }
         }
@@ -336,6 +336,9 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         const int zm = zs == 0 ? nz - 1 : zs - 1;
         if (active) load_words<S>(src, cxy + (int64_t)zm * zst, pa);
         int zn = zs;  // plane of the next prefetch (wrapped)
+        int64_t loff = cxy + (int64_t)zs * zst;  // its storage offset, advanced per plane
+        int64_t soff = loff;                      // storage offset of the next emitted plane
+        const int64_t wrap = (int64_t)nz * zst;
         int k3 = 0, k4 = 0;  // k % 3, k % 4
 
         if (owner) {
@@ -362,8 +365,12 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 }
                 if (own) {
                     if (k < last) {
-                        load_words<S>(src, cxy + (int64_t)zn * zst, nxt);
-                        zn = zn + 1 == nz ? 0 : zn + 1;
+                        load_words<S>(src, loff, nxt);
+                        loff += zst;
+                        if (++zn == nz) {
+                            zn = 0;
+                            loff -= wrap;
+                        }
                     }
                     arrive_own<S, TY>(cur, rho0, sc, up, flt, dn, col, c0, c5, c6);
                 }
@@ -373,7 +380,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                     if (own) {
                         const float *eup = up_base + (k4 >= 2 ? k4 - 2 : k4 + 2) * G::PLANE;  // plane k-2
                         const float *efl = fl_base + (k3 >= 1 ? k3 - 1 : 2) * G::PLANE;       // plane k-1
-                        const int64_t ai = cxy + (int64_t)z * zst;
+                        const int64_t ai = soff;
                         uint32_t wd = 0u;
                         bool exp = false;
                         unsigned bal = 0u;
@@ -418,6 +425,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                         }
                     }
                     if (k + 2 <= last) nb_arrive(3 + (k & 1), G::NTH);  // DONE(k)
+                    soff += zst;
                 }
                 wq = wnew;
                 rq = rnew;
@@ -440,8 +448,12 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 if (k >= 4) nb_sync(3 + (k & 1), G::NTH);  // DONE(k-2): ring slots of plane k are free
                 if (active) {
                     if (k < last) {
-                        load_words<S>(src, cxy + (int64_t)zn * zst, nxt);
-                        zn = zn + 1 == nz ? 0 : zn + 1;
+                        load_words<S>(src, loff, nxt);
+                        loff += zst;
+                        if (++zn == nz) {
+                            zn = 0;
+                            loff -= wrap;
+                        }
                     }
                     arrive_rim<S, TY>(cur, rho0, sc, rside, up_base + k4 * G::PLANE, fl_base + k3 * G::PLANE,
                                       dn_base + (k & 1) * G::PLANE, ccol);
@@ -598,6 +610,11 @@ cudaError_t launch_step(const StepLaunch &l, int storage, int tile_y, bool speci
                                                                   false, s)
                            : launch_s<__nv_bfloat16, false, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas,
                                                                    tile_y, l.full_tiles, s);
+        case MRLBM_STORAGE_F16_U32:
+            return special ? launch_s<HybridWord, true, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas, tile_y,
+                                                                  false, s)
+                           : launch_s<HybridWord, false, false>(ga, nullptr, l.parity, l.diag_part, l.n_ctas,
+                                                                   tile_y, l.full_tiles, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -623,6 +640,7 @@ cudaError_t prepare_step_batch(int storage, int tile_y) {
         case MRLBM_STORAGE_F32: return prepare_s<float>(tile_y);
         case MRLBM_STORAGE_F16: return prepare_s<__half>(tile_y);
         case MRLBM_STORAGE_BF16: return prepare_s<__nv_bfloat16>(tile_y);
+        case MRLBM_STORAGE_F16_U32: return prepare_s<HybridWord>(tile_y);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -639,6 +657,9 @@ cudaError_t launch_step_batch(const BatchArgs *ba, int parity, int storage, int 
         case MRLBM_STORAGE_BF16:
             return special ? launch_s<__nv_bfloat16, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, false, s)
                            : launch_s<__nv_bfloat16, false, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, false, s);
+        case MRLBM_STORAGE_F16_U32:
+            return special ? launch_s<HybridWord, true, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, false, s)
+                           : launch_s<HybridWord, false, true>(nullptr, ba, parity, nullptr, n_ctas, tile_y, false, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -662,6 +683,7 @@ int step_kernel_max_ctas_per_sm(int storage, int tile_y) {
         case MRLBM_STORAGE_F32: return occ_s<float>(tile_y);
         case MRLBM_STORAGE_F16: return occ_s<__half>(tile_y);
         case MRLBM_STORAGE_BF16: return occ_s<__nv_bfloat16>(tile_y);
+        case MRLBM_STORAGE_F16_U32: return occ_s<HybridWord>(tile_y);
         default: return 0;
     }
 }

@@ -37,6 +37,13 @@ __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return
 
 __host__ __device__ constexpr int scale_class(int field) { return field == 0 ? 0 : (field < 4 ? 1 : 2); }
 
+// Storage that keeps scaled deviations (every mode but FP32): the emit computes u and m with
+// their storage scales folded in and stores through store_scaled*.
+template <typename S>
+constexpr bool kScaled = !std::is_same<S, float>::value;
+template <typename S>
+constexpr bool kHybrid = std::is_same<S, HybridWord>::value;
+
 // Raw stored values -> moments (full rho).
 template <typename S>
 __device__ __forceinline__ Mom decode(const float v[10], float rho0, const StorageScale &sc) {
@@ -70,6 +77,11 @@ struct Raw<__half> {
 template <>
 struct Raw<__nv_bfloat16> {
     uint32_t w[5];
+};
+template <>
+struct Raw<HybridWord> {
+    float u[3];     // ux, uy, uz (FP32, unscaled)
+    uint32_t w[4];  // FP16 pairs (rho', mxx), (myy, mzz), (mxy, mxz), (myz, -)
 };
 
 // Populations of a node from its raw stored values: FP32 through the moments; 16-bit storage
@@ -157,12 +169,30 @@ __device__ __forceinline__ uint32_t sr_step_seed(uint32_t step) { return mix32(s
 
 // `ai` is the element index of field 0 of a node (aos_index); field k sits at
 // ai + field_offset(k): 32 k for FP32, 64 (k / 2) + k % 2 for FP16 / BF16 (ai is even there).
+// Hybrid: the 10 stored values of a node from its 3 FP32 words and 4 FP16 pair words.
+__device__ __forceinline__ void hybrid_values(const float u[3], const uint32_t w[4], float v[10]) {
+    const float2 a = pair_to_f<__half>(w[0]), b = pair_to_f<__half>(w[1]), c = pair_to_f<__half>(w[2]),
+                 d = pair_to_f<__half>(w[3]);
+    v[0] = a.x;
+    v[1] = u[0]; v[2] = u[1]; v[3] = u[2];
+    v[4] = a.y; v[5] = b.x; v[6] = b.y; v[7] = c.x; v[8] = c.y; v[9] = d.x;
+}
+
 template <typename S>
 __device__ __forceinline__ void load_raw(const S *__restrict__ base, int64_t ai, float v[10]) {
     if constexpr (std::is_same<S, float>::value) {
         const float *p = base + ai;
 #pragma unroll
         for (int k = 0; k < 10; ++k) v[k] = p[k * kXBlock];
+    } else if constexpr (kHybrid<S>) {
+        const uint32_t *p = reinterpret_cast<const uint32_t *>(base + ai);
+        float u[3];
+        uint32_t w[4];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) u[k] = __uint_as_float(p[k * kXBlock]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) w[k] = p[(3 + k) * kXBlock];
+        hybrid_values(u, w, v);
     } else {
         const uint32_t *p = reinterpret_cast<const uint32_t *>(base + ai);
 #pragma unroll
@@ -181,6 +211,12 @@ __device__ __forceinline__ void load_words(const S *__restrict__ base, int64_t a
         const float *p = base + ai;
 #pragma unroll
         for (int k = 0; k < 10; ++k) r.v[k] = p[k * kXBlock];
+    } else if constexpr (kHybrid<S>) {
+        const uint32_t *p = reinterpret_cast<const uint32_t *>(base + ai);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) r.u[k] = __uint_as_float(p[k * kXBlock]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) r.w[k] = p[(3 + k) * kXBlock];
     } else {
         const uint32_t *p = reinterpret_cast<const uint32_t *>(base + ai);
 #pragma unroll
@@ -193,6 +229,10 @@ template <typename S>
 __device__ __forceinline__ void rebuild(const Raw<S> &r, float rho0, const StorageScale &sc, float f[27]) {
     if constexpr (std::is_same<S, float>::value) {
         rebuild<S>(r.v, rho0, sc, f);
+    } else if constexpr (kHybrid<S>) {
+        float v[10];
+        hybrid_values(r.u, r.w, v);
+        rebuild<S>(v, rho0, sc, f);
     } else {
         float v[10];
 #pragma unroll
@@ -227,6 +267,15 @@ __device__ __forceinline__ void store_mom(S *__restrict__ base, int64_t ai, cons
         p[7 * kXBlock] = m.mxy;
         p[8 * kXBlock] = m.mxz;
         p[9 * kXBlock] = m.myz;
+    } else if constexpr (kHybrid<S>) {
+        uint32_t *w = reinterpret_cast<uint32_t *>(p);
+        w[0 * kXBlock] = __float_as_uint(m.ux * sc.s[1]);
+        w[1 * kXBlock] = __float_as_uint(m.uy * sc.s[1]);
+        w[2 * kXBlock] = __float_as_uint(m.uz * sc.s[1]);
+        w[3 * kXBlock] = pair_from_f<__half>((m.rho - rho0) * sc.s[0], m.mxx * sc.s[2]);
+        w[4 * kXBlock] = pair_from_f<__half>(m.myy * sc.s[2], m.mzz * sc.s[2]);
+        w[5 * kXBlock] = pair_from_f<__half>(m.mxy * sc.s[2], m.mxz * sc.s[2]);
+        w[6 * kXBlock] = pair_from_f<__half>(m.myz * sc.s[2], 0.0f);
     } else {
         uint32_t *w = reinterpret_cast<uint32_t *>(p);
         w[0 * kXBlock] = pair_from_f<S>((m.rho - rho0) * sc.s[0], m.ux * sc.s[1]);
@@ -244,6 +293,15 @@ __device__ __forceinline__ void store_mom_sr(S *__restrict__ base, int64_t ai, c
                                              const StorageScale &sc, uint32_t key) {
     if constexpr (std::is_same<S, float>::value) {
         store_mom<S>(base, ai, m, rho0, sc);
+    } else if constexpr (kHybrid<S>) {
+        uint32_t *w = reinterpret_cast<uint32_t *>(base + ai);
+        w[0 * kXBlock] = __float_as_uint(m.ux * sc.s[1]);
+        w[1 * kXBlock] = __float_as_uint(m.uy * sc.s[1]);
+        w[2 * kXBlock] = __float_as_uint(m.uz * sc.s[1]);
+        w[3 * kXBlock] = pair_from_f_sr<__half>((m.rho - rho0) * sc.s[0], m.mxx * sc.s[2], mix32(key));
+        w[4 * kXBlock] = pair_from_f_sr<__half>(m.myy * sc.s[2], m.mzz * sc.s[2], mix32(key + 0x9e3779b9u));
+        w[5 * kXBlock] = pair_from_f_sr<__half>(m.mxy * sc.s[2], m.mxz * sc.s[2], mix32(key + 0x3c6ef372u));
+        w[6 * kXBlock] = pair_from_f_sr<__half>(m.myz * sc.s[2], 0.0f, mix32(key + 0xdaa66d2bu));
     } else {
         uint32_t *w = reinterpret_cast<uint32_t *>(base + ai);
         w[0 * kXBlock] = pair_from_f_sr<S>((m.rho - rho0) * sc.s[0], m.ux * sc.s[1], mix32(key));
@@ -261,6 +319,16 @@ __device__ __forceinline__ void store_scaled(S *__restrict__ base, int64_t ai, c
                                              const StorageScale &sc) {
     static_assert(!std::is_same<S, float>::value, "FP32 storage holds physical moments");
     uint32_t *w = reinterpret_cast<uint32_t *>(base + ai);
+    if constexpr (kHybrid<S>) {
+        w[0 * kXBlock] = __float_as_uint(m.ux);
+        w[1 * kXBlock] = __float_as_uint(m.uy);
+        w[2 * kXBlock] = __float_as_uint(m.uz);
+        w[3 * kXBlock] = pair_from_f<__half>((m.rho - rho0) * sc.s[0], m.mxx);
+        w[4 * kXBlock] = pair_from_f<__half>(m.myy, m.mzz);
+        w[5 * kXBlock] = pair_from_f<__half>(m.mxy, m.mxz);
+        w[6 * kXBlock] = pair_from_f<__half>(m.myz, 0.0f);
+        return;
+    }
     w[0 * kXBlock] = pair_from_f<S>((m.rho - rho0) * sc.s[0], m.ux);
     w[1 * kXBlock] = pair_from_f<S>(m.uy, m.uz);
     w[2 * kXBlock] = pair_from_f<S>(m.mxx, m.myy);
@@ -272,11 +340,51 @@ __device__ __forceinline__ void store_scaled_sr(S *__restrict__ base, int64_t ai
                                                 const StorageScale &sc, uint32_t key) {
     static_assert(!std::is_same<S, float>::value, "FP32 storage holds physical moments");
     uint32_t *w = reinterpret_cast<uint32_t *>(base + ai);
+    if constexpr (kHybrid<S>) {
+        w[0 * kXBlock] = __float_as_uint(m.ux);
+        w[1 * kXBlock] = __float_as_uint(m.uy);
+        w[2 * kXBlock] = __float_as_uint(m.uz);
+        w[3 * kXBlock] = pair_from_f_sr<__half>((m.rho - rho0) * sc.s[0], m.mxx, mix32(key));
+        w[4 * kXBlock] = pair_from_f_sr<__half>(m.myy, m.mzz, mix32(key + 0x9e3779b9u));
+        w[5 * kXBlock] = pair_from_f_sr<__half>(m.mxy, m.mxz, mix32(key + 0x3c6ef372u));
+        w[6 * kXBlock] = pair_from_f_sr<__half>(m.myz, 0.0f, mix32(key + 0xdaa66d2bu));
+        return;
+    }
     w[0 * kXBlock] = pair_from_f_sr<S>((m.rho - rho0) * sc.s[0], m.ux, mix32(key));
     w[1 * kXBlock] = pair_from_f_sr<S>(m.uy, m.uz, mix32(key + 0x9e3779b9u));
     w[2 * kXBlock] = pair_from_f_sr<S>(m.mxx, m.myy, mix32(key + 0x3c6ef372u));
     w[3 * kXBlock] = pair_from_f_sr<S>(m.mzz, m.mxy, mix32(key + 0xdaa66d2bu));
     w[4 * kXBlock] = pair_from_f_sr<S>(m.mxz, m.myz, mix32(key + 0x78dde6e4u));
+}
+
+// One stored field of a node (the stored, scaled value) and its store: the layout of each
+// mode (field_offset for FP32 / FP16 / BF16; the hybrid mode's FP32 words and FP16 halves).
+template <typename S>
+__device__ __forceinline__ float load_field(const S *__restrict__ base, int64_t ai, int f) {
+    if constexpr (kHybrid<S>) {
+        const uint32_t *p = reinterpret_cast<const uint32_t *>(base + ai);
+        if (f >= 1 && f <= 3) return __uint_as_float(p[(f - 1) * kXBlock]);
+        const int k = f == 0 ? 0 : f - 3;  // half index among rho', mxx, myy, ..., myz
+        const __half *h = reinterpret_cast<const __half *>(p + (3 + (k >> 1)) * kXBlock);
+        return __half2float(h[k & 1]);
+    } else {
+        return to_f<S>(base[ai + field_offset(f, (int)sizeof(S))]);
+    }
+}
+template <typename S>
+__device__ __forceinline__ void store_field(S *__restrict__ base, int64_t ai, int f, float v) {
+    if constexpr (kHybrid<S>) {
+        uint32_t *p = reinterpret_cast<uint32_t *>(base + ai);
+        if (f >= 1 && f <= 3) {
+            p[(f - 1) * kXBlock] = __float_as_uint(v);
+            return;
+        }
+        const int k = f == 0 ? 0 : f - 3;
+        __half *h = reinterpret_cast<__half *>(p + (3 + (k >> 1)) * kXBlock);
+        h[k & 1] = __float2half_rn(v);
+    } else {
+        base[ai + field_offset(f, (int)sizeof(S))] = from_f<S>(v);
+    }
 }
 
 }  // namespace mrlbm

@@ -81,7 +81,7 @@ __global__ void init_kernel(const InitArgs a) {
         }
         default: break;
     }
-    const int64_t ai = aos_index(x, y, z, (a.nx + kXBlock - 1) / kXBlock, a.ny, (int)sizeof(S));
+    const int64_t ai = aos_at<S>(x, y, z, (a.nx + kXBlock - 1) / kXBlock, a.ny);
     store_mom<S>((S *)a.m_a, ai, m, a.rho0, a.sc);
     store_mom<S>((S *)a.m_b, ai, m, a.rho0, a.sc);
 }
@@ -94,20 +94,19 @@ __global__ void convert_kernel(const S *src, S *dst_a, S *dst_b, float *f32, uin
     if (i >= n) return;
     const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((int64_t)nx * ny));
     const int64_t h = layout == MRLBM_LAYOUT_REF_TILED ? ref_tiled_index(x, y, z, nx, ny) : i;
-    const int64_t ai = aos_index(x, y, z, (nx + kXBlock - 1) / kXBlock, ny, (int)sizeof(S));
+    const int64_t ai = aos_at<S>(x, y, z, (nx + kXBlock - 1) / kXBlock, ny);
     int slot = 0;
     for (int f = 0; f < 10; ++f) {
         if (!(mask & (1u << f))) continue;
         const float s = sc.s[scale_class(f)], is = sc.is[scale_class(f)];
-        const bool lowp = !std::is_same<S, float>::value;
+        const bool lowp = kScaled<S>;
         if (dir == 0) {
-            const float v = to_f<S>(src[ai + field_offset(f, (int)sizeof(S))]);
+            const float v = load_field<S>(src, ai, f);
             f32[(int64_t)slot * n + h] = lowp ? v * is : v;
         } else {
             const float v = f32[(int64_t)slot * n + h];
-            const S sv = from_f<S>(lowp ? v * s : v);
-            dst_a[ai + field_offset(f, (int)sizeof(S))] = sv;
-            if (dst_b) dst_b[ai + field_offset(f, (int)sizeof(S))] = sv;
+            store_field<S>(dst_a, ai, f, lowp ? v * s : v);
+            if (dst_b) store_field<S>(dst_b, ai, f, lowp ? v * s : v);
         }
         ++slot;
     }
@@ -141,6 +140,7 @@ cudaError_t launch_init(const InitArgs &a, int storage, cudaStream_t s) {
         case MRLBM_STORAGE_F32: init_kernel<float><<<blocks, 256, 0, s>>>(a); break;
         case MRLBM_STORAGE_F16: init_kernel<__half><<<blocks, 256, 0, s>>>(a); break;
         case MRLBM_STORAGE_BF16: init_kernel<__nv_bfloat16><<<blocks, 256, 0, s>>>(a); break;
+        case MRLBM_STORAGE_F16_U32: init_kernel<HybridWord><<<blocks, 256, 0, s>>>(a); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -163,6 +163,11 @@ cudaError_t launch_convert(const void *src, void *dst_a, void *dst_b, float *f32
         case MRLBM_STORAGE_BF16:
             convert_kernel<__nv_bfloat16><<<blocks, 256, 0, s>>>((const __nv_bfloat16 *)src, (__nv_bfloat16 *)dst_a,
                                                                  (__nv_bfloat16 *)dst_b, f32, field_mask, layout,
+                                                                 nx, ny, nz, sc, dir);
+            break;
+        case MRLBM_STORAGE_F16_U32:
+            convert_kernel<HybridWord><<<blocks, 256, 0, s>>>((const HybridWord *)src, (HybridWord *)dst_a,
+                                                                 (HybridWord *)dst_b, f32, field_mask, layout,
                                                                  nx, ny, nz, sc, dir);
             break;
         default: return cudaErrorInvalidValue;

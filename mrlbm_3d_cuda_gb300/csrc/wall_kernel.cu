@@ -208,8 +208,8 @@ __global__ void __launch_bounds__(128)
                 double fin[4] = {0.0, 0.0, 0.0, 0.0}, fo[4];
                 if (force) masked_momentum64(inm, m, fin);
                 collide(m, a.omega);
-                const int64_t ai = aos_index(x, y, z, a.nxb, a.ny, (int)sizeof(S));
-                if (sizeof(S) == 2 && a.sr_step)
+                const int64_t ai = aos_at<S>(x, y, z, a.nxb, a.ny);
+                if (kScaled<S> && a.sr_step)
                     store_mom_sr<S>((S *)a.m[parity ^ 1], ai, m, a.rho0, a.sc,
                                     sr_key(sr_step_seed(*a.sr_step), x, y, z, a.nx, a.ny));
                 else
@@ -267,6 +267,9 @@ cudaError_t launch_wall(const StepLaunch &l, int storage, int n_total, cudaStrea
         case MRLBM_STORAGE_BF16:
             wall_kernel<__nv_bfloat16, false><<<blocks, 128, 0, s>>>(l.ga, nullptr, l.parity, l.force);
             break;
+        case MRLBM_STORAGE_F16_U32:
+            wall_kernel<HybridWord, false><<<blocks, 128, 0, s>>>(l.ga, nullptr, l.parity, l.force);
+            break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -281,6 +284,9 @@ cudaError_t launch_wall_batch(const BatchArgs *ba, int parity, int force, int st
         case MRLBM_STORAGE_F16: wall_kernel<__half, true><<<n_blocks, 128, 0, s>>>(nullptr, ba, parity, f); break;
         case MRLBM_STORAGE_BF16:
             wall_kernel<__nv_bfloat16, true><<<n_blocks, 128, 0, s>>>(nullptr, ba, parity, f);
+            break;
+        case MRLBM_STORAGE_F16_U32:
+            wall_kernel<HybridWord, true><<<n_blocks, 128, 0, s>>>(nullptr, ba, parity, f);
             break;
         default: return cudaErrorInvalidValue;
     }

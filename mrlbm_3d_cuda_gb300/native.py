@@ -20,7 +20,7 @@ OK = 0
 ERR_INVALID_ARG, ERR_CUDA, ERR_DIVERGED, ERR_TIMEOUT, ERR_IO, ERR_UNSUPPORTED, ERR_STATE, ERR_NOMEM = (
     -1, -2, -3, -4, -5, -6, -7, -8)
 GEOM_NONE, GEOM_CYLINDER, GEOM_ANNULUS = 0, 1, 2
-STORAGE_F32, STORAGE_F16, STORAGE_BF16 = 0, 1, 2
+STORAGE_F32, STORAGE_F16, STORAGE_BF16, STORAGE_F16_U32 = 0, 1, 2, 3
 MASS_EQUILIBRIUM, MASS_STRONG = 0, 1
 INIT_REFERENCE_NOISE, INIT_REST, INIT_TAYLOR_GREEN, INIT_UNIFORM, INIT_NOISY_UNIFORM = 0, 1, 2, 3, 4
 LAYOUT_LEXICOGRAPHIC, LAYOUT_REF_TILED = 0, 1

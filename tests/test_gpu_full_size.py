@@ -82,10 +82,14 @@ def test_largest_single_gpu_grid_shift_invariance(cuda_device):
     assert abs(diag[-1, 0] - diag[0, 0]) / (1024 * 512 * 256) < 1e-6 * steps
 
 
-C2_STORAGE = {"f32": (0, 0), "f16": (1, 0), "f16sr": (1, 1), "bf16": (2, 0), "bf16sr": (2, 1)}
-# max over t of |E/E64 - 1| and of |eps - eps64| / max eps64 (eps = -dE/dt over 50 steps)
-C2_BOUND = {"f32": (1e-5, 1e-3), "f16": (5e-2, 1.0), "f16sr": (2e-3, 5e-2), "bf16": (0.3, 3.0),
-            "bf16sr": (2e-2, 0.3)}
+C2_STORAGE = {"f32": (0, 0), "f16": (1, 0), "f16sr": (1, 1), "bf16": (2, 0), "bf16sr": (2, 1), "f16u32": (3, 0),
+              "f16u32sr": (3, 1)}
+# max over t of |E/E64 - 1| and of |eps - eps64| / max eps64 (eps = -dE/dt over 50 steps),
+# about three times the GB300 measurement: FP32 4.7e-6 / 3.8e-5, FP16 6.4e-3 / 0.144, FP16 sr
+# 3.2e-4 / 2.2e-3, BF16 0.198 / 3.08 (its decay goes wrong: bounded only against breakage),
+# BF16 sr 2.0e-4 / 1.2e-2
+C2_BOUND = {"f32": (1.5e-5, 1.2e-4), "f16": (2e-2, 0.45), "f16sr": (1e-3, 7e-3), "bf16": (0.6, 10.0),
+            "bf16sr": (6e-4, 4e-2), "f16u32": (2e-2, 0.45), "f16u32sr": (1e-3, 7e-3)}
 
 
 @pytest.mark.parametrize("storage", list(C2_STORAGE))

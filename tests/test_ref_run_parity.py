@@ -200,7 +200,8 @@ def test_taylor_green_256_matches_reference_build(cuda_device):
     check_field_stats(m, g, (0, 1, 2, 4, 5, 7), sumsq=True)
 
 
-SHEDDING_STORAGE = [("f32", 0, 0), ("f16", 1, 0), ("f16_sr", 1, 1), ("bf16", 2, 0), ("bf16_sr", 2, 1)]
+SHEDDING_STORAGE = [("f32", 0, 0), ("f16", 1, 0), ("f16_sr", 1, 1), ("bf16", 2, 0), ("bf16_sr", 2, 1),
+                    ("f16u32", 3, 0), ("f16u32_sr", 3, 1)]
 
 
 def test_shedding_statistics_match_reference_build(cuda_device):

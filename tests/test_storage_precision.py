@@ -22,7 +22,8 @@ import pytest
 from conftest import field_errors, record_parity
 
 pytestmark = pytest.mark.gpu
-STORAGE = {"f32": (0, 0), "f16": (1, 0), "bf16": (2, 0), "f16sr": (1, 1), "bf16sr": (2, 1)}
+STORAGE = {"f32": (0, 0), "f16": (1, 0), "bf16": (2, 0), "f16sr": (1, 1), "bf16sr": (2, 1), "f16u32": (3, 0),
+           "f16u32sr": (3, 1)}
 
 
 def make(fn, storage, *args, **kw):
@@ -55,6 +56,7 @@ def tgv_oracle(cuda_device):
 
 
 @pytest.mark.parametrize("storage,e_tol,eps_tol", [("f32", 1e-5, 1e-4), ("f16", 2e-3, 4e-2), ("bf16", 6e-2, 0.8),
+                                                   ("f16u32", 2e-3, 4e-2), ("f16u32sr", 1e-4, 4e-3),
                                                    ("f16sr", 1e-4, 4e-3), ("bf16sr", 1e-3, 3e-2)])
 def test_taylor_green_energy_decay(tgv_oracle, storage, e_tol, eps_tol):
     from mrlbm_3d_cuda_gb300 import Simulation, cases
@@ -91,6 +93,7 @@ def cylinder_oracle(cuda_device):
 
 
 @pytest.mark.parametrize("storage,tol", [("f32", 1e-4), ("f16", 5e-3), ("bf16", 1.5e-2), ("f16sr", 2e-4),
+                                         ("f16u32", 5e-3), ("f16u32sr", 2e-4),
                                          ("bf16sr", 5e-4)])
 def test_cylinder_drag_within_half_percent(cylinder_oracle, storage, tol):
     """Cd = 2 Fx / (rho0 U^2 D NZ), mean over steps 1500..1999, within 0.5 % of FP64 (tighter
@@ -109,7 +112,8 @@ def test_cylinder_drag_within_half_percent(cylinder_oracle, storage, tol):
     assert abs(cd / cd64 - 1) < tol, (storage, cd, cd64)
 
 
-@pytest.mark.parametrize("storage,tol", [("f32", 1e-3), ("f16", 4e-2), ("f16sr", 5e-3), ("bf16sr", 3e-3)])
+@pytest.mark.parametrize("storage,tol", [("f32", 1e-3), ("f16", 4e-2), ("f16sr", 5e-3), ("bf16sr", 3e-3),
+                                         ("f16u32", 4e-2), ("f16u32sr", 5e-3)])
 def test_annulus_torque(cuda_device, storage, tol):
     import oracle
     from mrlbm_3d_cuda_gb300 import Simulation, cases
@@ -130,7 +134,7 @@ def test_annulus_torque(cuda_device, storage, tol):
     assert abs(t[0] / t64[0] - 1) < tol, (t, t64)
 
 
-@pytest.mark.parametrize("storage", ["f16sr", "bf16sr"])
+@pytest.mark.parametrize("storage", ["f16sr", "bf16sr", "f16u32sr"])
 def test_stochastic_rounding_is_reproducible(cuda_device, storage, tmp_path, monkeypatch):
     """The random bits depend only on the node, the field pair and the step number, so a
     stochastically rounded run is bit-identical across tilings, across a checkpoint reload,
@@ -189,8 +193,11 @@ def tgv_oracle_fields(cuda_device):
 
 
 # Per-field error bounds against the FP64 oracle (scaled metric of conftest.field_errors:
-# max |a - b| / max(||b||inf, s_f), s_f = 1 for rho, U for u, cs2 for m).
-FIELD_BOUND = {"f32": 2e-5, "f16": 5e-2, "f16sr": 5e-2, "bf16": 0.5, "bf16sr": 0.5}
+# max |a - b| / max(||b||inf, s_f), s_f = 1 for rho, U for u, cs2 for m), about three times the
+# worst field measured on a GB300 over the two cases (FP32 2.1e-5, FP16 8.3e-3, FP16 sr 1.0e-2,
+# BF16 0.41, BF16 sr 8.7e-2: the velocity fields of the Taylor-Green run).
+FIELD_BOUND = {"f32": 6e-5, "f16": 2.5e-2, "f16sr": 3e-2, "bf16": 1.0, "bf16sr": 0.25, "f16u32": 2.5e-2,
+               "f16u32sr": 3e-2}
 
 
 @pytest.mark.parametrize("storage", list(STORAGE))
