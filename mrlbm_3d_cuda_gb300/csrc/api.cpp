@@ -213,7 +213,9 @@ int setup_tiling(mrlbm_handle *h, int ty, int lz) {
                 for (int x = x0; x < std::min(d.nx, x0 + TILE_X); ++x) {
                     const int64_t i = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
                     const uint32_t wd = word[i];
-                    if (wd == 0u || (wd & NW_FROZEN)) continue;
+                    // plain fluid nodes marked only as wall-stencil nodes are updated (and
+                    // snapshotted) by the step kernel itself
+                    if (wd == 0u || wd == NW_STENCIL || (wd & NW_FROZEN)) continue;
                     const uint64_t p = (uint64_t)x | ((uint64_t)y << 21) | ((uint64_t)z << 42);
                     if ((wd & NW_CLASS_MASK) == C_SOLID) {
                         solid_xyz.push_back(p);

@@ -195,6 +195,19 @@ __device__ __forceinline__ void arrive_rim(const Raw<S> &raw, float rho0, const 
     }
 }
 
+// Post-stream (pre-collision) moments of a wall-stencil node into its side-buffer entry, the
+// snapshot the wall kernel interpolates from (the node-list kernel writes the same for the
+// marked nodes it handles); iu / im undo the storage scales of the 16-bit emit.
+template <int TY>
+__device__ __forceinline__ void snapshot_t(float *side, int slot, int x, int y, int z, int x0, int y0, int nz,
+                                           const Mom &m, float rho0, float iu, float im) {
+    float *e = side + side_index(slot, x, y, z, x0, y0, nz, TILE_X, TY) * 16;
+    e[0] = m.rho - rho0;
+    e[1] = m.ux * iu; e[2] = m.uy * iu; e[3] = m.uz * iu;
+    e[4] = m.mxx * im; e[5] = m.myy * im; e[6] = m.mzz * im;
+    e[7] = m.mxy * im; e[8] = m.mxz * im; e[9] = m.myz * im;
+}
+
 // Named CTA barriers (PTX bar.sync / bar.arrive; id 0 is __syncthreads).  A generation
 // completes when `n` threads (whole warps) have arrived; bar.arrive does not wait.
 __device__ __forceinline__ void nb_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
@@ -232,6 +245,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
     const int32_t *__restrict__ tile_slot = nullptr;
     const uint32_t *__restrict__ word = nullptr;
     float *__restrict__ popbuf = nullptr;
+    float *__restrict__ side = nullptr;  // wall-stencil snapshots of special tiles
     int n_pop = 0;
     const int32_t *__restrict__ row_base = nullptr;
     float omega = 1.f, rho0 = 1.f;
@@ -252,6 +266,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
         tile_slot = c->tile_slot;
         word = c->word;
         popbuf = c->popbuf;
+        side = c->side;
         n_pop = c->n_list_pop;
         row_base = c->row_base;
         omega = c->omega;
@@ -387,14 +402,20 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                         if constexpr (SPECIAL) {
                             if (slot >= 0) {
                                 wd = wq;
-                                exp = wd != 0u && !(wd & NW_FROZEN) && (wd & NW_CLASS_MASK) != C_SOLID;
+                                // a plain fluid node whose only mark is the wall-stencil bit is
+                                // updated here, like any bulk node, plus its snapshot; every other
+                                // marked node goes to the node-list kernel
+                                exp = wd != 0u && wd != NW_STENCIL && !(wd & NW_FROZEN) &&
+                                      (wd & NW_CLASS_MASK) != C_SOLID;
                                 bal = __ballot_sync(row_mask, exp);
                             }
                         }
-                        if (wd == 0u) {
+                        const bool snap = SPECIAL && wd == NW_STENCIL;
+                        if (wd == 0u || snap) {
                             Mom m;
                             if constexpr (std::is_same<S, float>::value) {
                                 gather_evaluate<TY>(eup, efl, dn, col, p0, pp5, c6, m);
+                                if (snap) snapshot_t<TY>(side, slot, x, y, z, x0, y0, nz, m, rho0, 1.0f, 1.0f);
                                 if (diag) {
                                     dm += m.rho - rho0;
                                     de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
@@ -405,6 +426,7 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                                 // u and m come out with their storage scales: no unscaling on
                                 // the way in (rebuild) and no scaling on the way out
                                 gather_evaluate<TY, true>(eup, efl, dn, col, p0, pp5, c6, m, sc.s[1], sc.s[2]);
+                                if (snap) snapshot_t<TY>(side, slot, x, y, z, x0, y0, nz, m, rho0, sc.is[1], sc.is[2]);
                                 if (diag) {
                                     dm += m.rho - rho0;
                                     de += 0.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz) * (sc.is[1] * sc.is[1]);

@@ -164,10 +164,15 @@ def test_reference_cylinder_case(cuda_device, steps):
 
 
 def test_annulus_two_walls(cuda_device):
+    """Both walls' torques after 1000 steps.  Earlier the outer wall's torque is the arrival
+    of the diffusion front started at the inner wall: a small difference of nearly equal
+    in / out momenta that FP32 rounding moves by percents (the FP32 oracle is 0.5 % from the
+    FP64 one at 200 steps and 3.8 % at 400; rounding-sized perturbations of the initial state
+    move it by up to 1.4 % at 200), so it is no parity check there."""
     from mrlbm_3d_cuda_gb300 import cases
     from mrlbm_3d_cuda_gb300 import native as N
     desc = cases.annulus(48, 48, 8, 8.0, 20.0, 0.05, 50.0)
-    res = run_pair(desc, 200, N.INIT_REST, forces=True)
+    res = run_pair(desc, 1000, N.INIT_REST, forces=True)
     assert_fields(res, 0.05)
     for w in range(2):
         assert_forces(res, w, comps=(4,))

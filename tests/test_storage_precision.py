@@ -10,10 +10,14 @@ each storage mode:
 |---|---|---|---|---|---|
 | Taylor-Green 64^3, Re 1600, 1000 steps | max_t abs(E/E64 - 1) | 6.9e-4 | 2.9e-5 | 3.0e-2 | 2.9e-4 |
 | same | max_t abs(eps - eps64) / max eps64 | 1.8e-2 | 1.4e-3 | 0.41 | 1.1e-2 |
-| cylinder 128x64x32, Re 100, 2000 steps | Cd (mean of last 500 steps) rel. error | 5.7e-4 | 2e-7 | 4.7e-3, 6.9e-3 | 9.8e-5 |
-| annulus 48x48x8, r 8 / 20, 2000 steps | inner-wall torque rel. error | 1.3e-2 | 1.4e-3 | 0.21 | 6.4e-4 |
+| cylinder 128x64x32, Re 100, 2000 steps | Cd (mean of last 500 steps) rel. error | 5.7e-4 | 2e-7 | 4.7e-3, 6.9e-3 | <= 2.0e-3 (*) |
+| annulus 48x48x8, r 8 / 20, 2000 steps | inner-wall torque rel. error | 1.3e-2 | 1.4e-3 | 0.21 | <= 6.7e-3 (*) |
 
-FP32 storage stays within 1e-5 of FP64 on all of them."""
+FP32 storage stays within 1e-5 of FP64 on all of them.  (*) BF16 with stochastic rounding:
+the largest of eight realisations (rest state plus a 1e-6 density perturbation from eight
+seeds, two builds of the step whose FP32 arithmetic differs in the last bit); single
+realisations ranged from 4e-5 to 2.0e-3 (Cd) and 1.3e-4 to 6.7e-3 (torque), so the
+bounds hold the spread, not one draw."""
 from __future__ import annotations
 
 import numpy as np
@@ -94,7 +98,7 @@ def cylinder_oracle(cuda_device):
 
 @pytest.mark.parametrize("storage,tol", [("f32", 1e-4), ("f16", 5e-3), ("bf16", 1.5e-2), ("f16sr", 2e-4),
                                          ("f16u32", 5e-3), ("f16u32sr", 2e-4),
-                                         ("bf16sr", 5e-4)])
+                                         ("bf16sr", 4e-3)])
 def test_cylinder_drag_within_half_percent(cylinder_oracle, storage, tol):
     """Cd = 2 Fx / (rho0 U^2 D NZ), mean over steps 1500..1999, within 0.5 % of FP64 (tighter
     for FP32 and stochastic rounding).  BF16 with round-to-nearest sits at the edge of the
@@ -112,7 +116,7 @@ def test_cylinder_drag_within_half_percent(cylinder_oracle, storage, tol):
     assert abs(cd / cd64 - 1) < tol, (storage, cd, cd64)
 
 
-@pytest.mark.parametrize("storage,tol", [("f32", 1e-3), ("f16", 4e-2), ("f16sr", 5e-3), ("bf16sr", 3e-3),
+@pytest.mark.parametrize("storage,tol", [("f32", 1e-3), ("f16", 4e-2), ("f16sr", 5e-3), ("bf16sr", 1.5e-2),
                                          ("f16u32", 4e-2), ("f16u32sr", 5e-3)])
 def test_annulus_torque(cuda_device, storage, tol):
     import oracle
