@@ -116,37 +116,70 @@ __device__ __forceinline__ ClassSums class_sums(float mm, float m0, float mp, fl
     return s;
 }
 
+// Packed FP32 (sm_100+ add / sub .rn.f32x2): one instruction, two independently IEEE-rounded
+// lanes, so a packed sum gives bit for bit the two scalar sums.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    unsigned long long ra, rb, rd;
+    memcpy(&ra, &a, 8);
+    memcpy(&rb, &b, 8);
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+    float2 d;
+    memcpy(&d, &rd, 8);
+    return d;
+}
+
+// class_sums of two classes at once (lane x, lane y), the same operations in the same order
+struct ClassSums2 {
+    float2 s0, sx, sy, sxx, syy, sxy;
+};
+__device__ __forceinline__ ClassSums2 class_sums2(float2 mm, float2 m0, float2 mp, float2 zm, float2 zz, float2 zp,
+                                                  float2 pm, float2 p0, float2 pp) {
+    const float2 rp = add2(add2(mp, zp), pp), r0 = add2(add2(m0, zz), p0), rm = add2(add2(mm, zm), pm);
+    const float2 cp = add2(add2(pm, p0), pp), cm = add2(add2(mm, m0), mp);
+    ClassSums2 s;
+    s.s0 = add2(add2(rp, r0), rm);
+    s.sx = sub2(cp, cm);
+    s.sxx = add2(cp, cm);
+    s.sy = sub2(rp, rm);
+    s.syy = add2(rp, rm);
+    s.sxy = sub2(add2(pp, mm), add2(pm, mp));
+    return s;
+}
+
 // Gather the pulled populations of the owner node and evaluate its moments on the fly,
-// class by class (c_z = +1 from plane z-1, 0 from z, -1 from z+1).
+// class by class (c_z = +1 from plane z-1, 0 from z, -1 from z+1); the c_z = +1 and c_z = 0
+// classes share packed sums (lane x: +1, lane y: 0).
 // SCALED: u and the second moments come out multiplied by the storage scales su and sm.
 template <int TY, bool SCALED = false>
 __device__ __forceinline__ void gather_evaluate(const float *up, const float *fl, const float *dn, int col, float f0,
                                                 float f5, float f6, Mom &m, float su = 1.0f, float sm = 1.0f) {
 #define MRLBM_P(q) pull<q, TY>(up, fl, dn, col)
-    // c_z = +1: (cx,cy) = (-1,-1) 22, (-1,0) 16, (-1,1) 25, (0,-1) 18, (0,0) 5, (0,1) 11, (1,-1) 23, (1,0) 9, (1,1) 19
-    const ClassSums u = class_sums(MRLBM_P(22), MRLBM_P(16), MRLBM_P(25), MRLBM_P(18), f5, MRLBM_P(11), MRLBM_P(23),
-                                   MRLBM_P(9), MRLBM_P(19));
-    // c_z = 0: 8, 2, 14, 4, 0, 3, 13, 1, 7
-    const ClassSums c = class_sums(MRLBM_P(8), MRLBM_P(2), MRLBM_P(14), MRLBM_P(4), f0, MRLBM_P(3), MRLBM_P(13),
-                                   MRLBM_P(1), MRLBM_P(7));
+#define MRLBM_P2(a, b) make_float2(MRLBM_P(a), MRLBM_P(b))
+    // (c_x, c_y) = (-1,-1), (-1,0), (-1,1), (0,-1), (0,0), (0,1), (1,-1), (1,0), (1,1):
+    // c_z = +1: 22, 16, 25, 18, 5, 11, 23, 9, 19;  c_z = 0: 8, 2, 14, 4, 0, 3, 13, 1, 7
+    const ClassSums2 uc = class_sums2(MRLBM_P2(22, 8), MRLBM_P2(16, 2), MRLBM_P2(25, 14), MRLBM_P2(18, 4),
+                                      make_float2(f5, f0), MRLBM_P2(11, 3), MRLBM_P2(23, 13), MRLBM_P2(9, 1),
+                                      MRLBM_P2(19, 7));
     // c_z = -1: 20, 10, 24, 12, 6, 17, 26, 15, 21
     const ClassSums d = class_sums(MRLBM_P(20), MRLBM_P(10), MRLBM_P(24), MRLBM_P(12), f6, MRLBM_P(17), MRLBM_P(26),
                                    MRLBM_P(15), MRLBM_P(21));
+#undef MRLBM_P2
 #undef MRLBM_P
-    const float rho = (u.s0 + c.s0) + d.s0;
+    const float rho = (uc.s0.x + uc.s0.y) + d.s0;
     const float inv = __frcp_rn(rho);  // correctly rounded, as 1.0f / rho
     const float iu = SCALED ? __fmul_rn(inv, su) : inv, im = SCALED ? __fmul_rn(inv, sm) : inv;
     const float cs = SCALED ? __fmul_rn(-kCs2, sm) : -kCs2;
     m.rho = rho;
-    m.ux = ((u.sx + c.sx) + d.sx) * iu;
-    m.uy = ((u.sy + c.sy) + d.sy) * iu;
-    m.uz = (u.s0 - d.s0) * iu;
-    m.mxx = __fmaf_rn((u.sxx + c.sxx) + d.sxx, im, cs);
-    m.myy = __fmaf_rn((u.syy + c.syy) + d.syy, im, cs);
-    m.mzz = __fmaf_rn(u.s0 + d.s0, im, cs);
-    m.mxy = ((u.sxy + c.sxy) + d.sxy) * im;
-    m.mxz = (u.sx - d.sx) * im;
-    m.myz = (u.sy - d.sy) * im;
+    m.ux = ((uc.sx.x + uc.sx.y) + d.sx) * iu;
+    m.uy = ((uc.sy.x + uc.sy.y) + d.sy) * iu;
+    m.uz = (uc.s0.x - d.s0) * iu;
+    m.mxx = __fmaf_rn((uc.sxx.x + uc.sxx.y) + d.sxx, im, cs);
+    m.myy = __fmaf_rn((uc.syy.x + uc.syy.y) + d.syy, im, cs);
+    m.mzz = __fmaf_rn(uc.s0.x + d.s0, im, cs);
+    m.mxy = ((uc.sxy.x + uc.sxy.y) + d.sxy) * im;
+    m.mxz = (uc.sx.x - d.sx) * im;
+    m.myz = (uc.sy.x - d.sy) * im;
 }
 
 template <int TY>
