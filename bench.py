@@ -405,15 +405,18 @@ STATED_ERRORS = {"f32": {"c1_cd_rel_err": 1.0e-5, "tgv64_energy_rel_err": 1.0e-6
 
 
 def storage_comparison(args, stream, n, world):
-    """The same Taylor-Green step with FP16 storage, rounding to nearest and stochastically:
-    device-resident MLUPS over min(steps, 1000) timed steps, beside the stated errors."""
+    """The same Taylor-Green step with FP16 storage and with the hybrid storage (FP32
+    velocity, FP16 density deviation and second moments), each rounding to nearest and
+    stochastically: device-resident MLUPS over min(steps, 1000) timed steps, beside the stated
+    errors."""
     import torch
     from mrlbm_3d_cuda_gb300 import Simulation, cases
     from mrlbm_3d_cuda_gb300 import native as N
     out = {}
     k = max(1, min(args.steps, 1000))
-    for name, sr in (("f16", 0), ("f16_sr", 1)):
-        desc = cases.c2_taylor_green(n, STORAGE["f16"])
+    for name, st, sr in (("f16", "f16", 0), ("f16_sr", "f16", 1), ("f16u32", "f16u32", 0),
+                         ("f16u32_sr", "f16u32", 1)):
+        desc = cases.c2_taylor_green(n, STORAGE[st])
         desc.stochastic_rounding = sr
         sim = Simulation(desc, init=False)
         sim.set_stream(stream.cuda_stream)
@@ -430,8 +433,8 @@ def storage_comparison(args, stream, n, world):
         value = replica_value(nodes, k, ms * 1e-3, world)
         peak, _ = measured_peaks()
         out[name] = {"value": value, "unit": "MLUPS", "steps": k,
-                     "frac_vs_min_traffic": nodes * B_MIN["f16"] / (ms / k * 1e-3) / 1e9 / peak,
-                     **STATED_ERRORS[name]}
+                     "frac_vs_min_traffic": nodes * B_MIN[st] / (ms / k * 1e-3) / 1e9 / peak,
+                     **STATED_ERRORS.get(name, {})}
         sim.close()
     out["f32"] = dict(STATED_ERRORS["f32"])
     out["errors_from"] = "tests/test_storage_precision.py: GB300 runs against the FP64 oracle"

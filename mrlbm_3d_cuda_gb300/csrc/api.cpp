@@ -195,13 +195,12 @@ int setup_tiling(mrlbm_handle *h, int ty, int lz) {
     h->n_special = n_special;
 
     // Non-bulk nodes of special tiles, in the order the step kernel exports their pulled
-    // populations: slot, z, tile row, x.  Solid nodes of updated blocks need no populations
-    // and follow the others; frozen nodes are never updated and are in no list.
+    // populations: slot, z, tile row, x.  Solid nodes of updated blocks need no populations:
+    // the step kernel collides them in place; frozen nodes are never updated.  Neither is
+    // in the list.
     std::vector<uint64_t> list_xyz;
     std::vector<uint32_t> list_word;
     std::vector<int32_t> row_base((size_t)n_special * d.nz * h->tile_y, 0);
-    std::vector<uint64_t> solid_xyz;
-    std::vector<uint32_t> solid_word;
     for (int t = 0; t < tiles; ++t) {
         if (slot[t] < 0) continue;
         const int x0 = (t % h->tiles_x) * TILE_X, y0 = (t / h->tiles_x) * h->tile_y;
@@ -216,23 +215,16 @@ int setup_tiling(mrlbm_handle *h, int ty, int lz) {
                     // plain fluid nodes marked only as wall-stencil nodes are updated (and
                     // snapshotted) by the step kernel itself
                     if (wd == 0u || wd == NW_STENCIL || (wd & NW_FROZEN)) continue;
-                    const uint64_t p = (uint64_t)x | ((uint64_t)y << 21) | ((uint64_t)z << 42);
-                    if ((wd & NW_CLASS_MASK) == C_SOLID) {
-                        solid_xyz.push_back(p);
-                        solid_word.push_back(wd);
-                    } else {
-                        list_xyz.push_back(p);
-                        list_word.push_back(wd);
-                    }
+                    if ((wd & NW_CLASS_MASK) == C_SOLID) continue;
+                    list_xyz.push_back((uint64_t)x | ((uint64_t)y << 21) | ((uint64_t)z << 42));
+                    list_word.push_back(wd);
                 }
             }
     }
-    if (list_xyz.size() + solid_xyz.size() >= (size_t)INT32_MAX / 27)
+    if (list_xyz.size() >= (size_t)INT32_MAX / 27)
         return fail(h, MRLBM_ERR_INVALID_ARG, "too many boundary nodes");
     h->n_list_pop = (int)list_xyz.size();
-    list_xyz.insert(list_xyz.end(), solid_xyz.begin(), solid_xyz.end());
-    list_word.insert(list_word.end(), solid_word.begin(), solid_word.end());
-    h->n_list = (int)list_xyz.size();
+    h->n_list = h->n_list_pop;
     h->n_list_blocks = special_list_blocks(h->n_list);
     const int nseg = (d.nz + h->lz - 1) / h->lz;
     // work items are int32 `tile | segment << 20` (decoded in step_kernel)

@@ -82,9 +82,9 @@ struct StepArgs {
     WallArgs wall[2];
     const uint32_t *tag_in = nullptr, *tag_out = nullptr;  // [256] BCFLUID masks
     int *error = nullptr;     // sticky device error flag
-    // non-bulk node list (special tiles only): entries [0, n_list_pop) get their 27 pulled
-    // populations from the step kernel, in (tile slot, z, tile row, x) order; entries
-    // [n_list_pop, n_list) are solid nodes of updated blocks (no populations)
+    // non-bulk node list (special tiles only): every entry gets its 27 pulled populations
+    // from the step kernel, in (tile slot, z, tile row, x) order (n_list == n_list_pop;
+    // plain stencil nodes and solid nodes are updated by the step kernel itself)
     const uint64_t *list_xyz = nullptr;   // x | y << 21 | z << 42
     const uint32_t *list_word = nullptr;  // node word of each entry
     int n_list_pop = 0, n_list = 0;

@@ -161,13 +161,8 @@ __global__ void __launch_bounds__(kListThreads)
         const int x = (int)(p & 0x1FFFFFu), y = (int)((p >> 21) & 0x1FFFFFu), z = (int)(p >> 42);
         const uint32_t w = a.list_word[i];
         float f[27];
-        if (i < n_pop) {
 #pragma unroll
-            for (int q = 0; q < 27; ++q) f[q] = a.popbuf[(int64_t)q * n_pop + i];
-        } else {
-#pragma unroll
-            for (int q = 0; q < 27; ++q) f[q] = 0.f;  // solid nodes use no populations
-        }
+        for (int q = 0; q < 27; ++q) f[q] = a.popbuf[(int64_t)q * n_pop + i];
         const int tx = x / TILE_X, ty = y / a.tile_y;
         const int slot = a.tile_slot[ty * a.tiles_x + tx];
         Mom m;

@@ -477,6 +477,16 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                             float *pq = popbuf + (rq + __popc(bal & ((1u << tx) - 1u)));
 #pragma unroll
                             for (int q = 0; q < 27; ++q) pq[(int64_t)q * n_pop] = fw[q];
+                        } else if (SPECIAL && (wd & NW_CLASS_MASK) == C_SOLID && !(wd & NW_FROZEN)) {
+                            // solid node of an updated block: its pre-stream moments, collided
+                            // (the reference collides every node of an active block)
+                            Mom m = load_mom<S>(src, ai, rho0, sc);
+                            if (wd & NW_STENCIL) snapshot_t<TY>(side, slot, x, y, z, x0, y0, nz, m, rho0, 1.0f, 1.0f);
+                            collide(m, omega);
+                            if (kScaled<S> && sr_on)
+                                store_mom_sr<S>(dst, ai, m, rho0, sc, sr_key(sr_seed, x, y, z, nx, ny));
+                            else
+                                store_mom<S>(dst, ai, m, rho0, sc);
                         }
                     }
                     if (k + 2 <= last) nb_arrive(3 + (k & 1), G::NTH);  // DONE(k)
