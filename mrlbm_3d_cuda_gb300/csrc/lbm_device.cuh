@@ -467,27 +467,23 @@ __device__ __forceinline__ void incoming_rotated(float nx, float ny, uint32_t ma
     o.myz = syz * inv;
 }
 
-// Momentum and mass carried by the populations of `mask`, rebuilt from the moments in FP64
-// (compute_forces_mass, forces.cu:3-23, does this in float; the difference of the incoming and
-// outgoing sums cancels most digits, so the force integration runs in double here).
-static __device__ __noinline__ void masked_momentum64(uint32_t mask, const Mom &m, double out[4]) {
-    const double ux = 3.0 * m.ux, uy = 3.0 * m.uy, uz = 3.0 * m.uz;
-    const double xx = 4.5 * m.mxx, yy = 4.5 * m.myy, zz = 4.5 * m.mzz;
-    const double xy = 9.0 * m.mxy, xz = 9.0 * m.mxz, yz = 9.0 * m.myz;
-    const double p0 = 1.0 - (xx + yy + zz) / 3.0;
-    double fx = 0.0, fy = 0.0, fz = 0.0, fm = 0.0;
+// Momentum and mass carried by the populations of `mask` at one node, as
+// compute_forces_mass (forces.cu:3-23) forms them: the populations rebuilt from the moments in
+// FP32 and summed in FP32 in direction order.  The callers take the node's incoming minus
+// outgoing sums and accumulate the nodes in FP64 (the reference accumulates FP32 atomics);
+// FP64 per population would cost ~200 FP64 operations per node on a part whose FP64 rate is
+// a small fraction of its FP32 rate.
+static __device__ __noinline__ void masked_momentum(uint32_t mask, const Mom &m, double out[4]) {
+    float f[27];
+    reconstruct(m, f);
+    float fx = 0.f, fy = 0.f, fz = 0.f, fm = 0.f;
+#pragma unroll
     for (int q = 0; q < 27; ++q) {
         if (!(mask & (1u << q))) continue;
-        const int cx = cxq(q), cy = cyq(q), cz = czq(q);
-        const int n2 = cx * cx + cy * cy + cz * cz;
-        const double w = n2 == 0 ? 8.0 / 27.0 : n2 == 1 ? 2.0 / 27.0 : n2 == 2 ? 1.0 / 54.0 : 1.0 / 216.0;
-        const double f = (double)m.rho * w *
-                         (p0 + cx * ux + cy * uy + cz * uz + cx * cx * xx + cy * cy * yy + cz * cz * zz +
-                          cx * cy * xy + cx * cz * xz + cy * cz * yz);
-        fx += f * cx;
-        fy += f * cy;
-        fz += f * cz;
-        fm += f;
+        fx = __fadd_rn(fx, __fmul_rn(f[q], (float)cxq(q)));
+        fy = __fadd_rn(fy, __fmul_rn(f[q], (float)cyq(q)));
+        fz = __fadd_rn(fz, __fmul_rn(f[q], (float)czq(q)));
+        fm = __fadd_rn(fm, f[q]);
     }
     out[0] = fx;
     out[1] = fy;

@@ -124,11 +124,11 @@ __device__ __forceinline__ int special_node(const StepArgs &a, int parity, bool 
     const bool bcf = force && slot >= 0 && (cls == C_BCFLUID_INNER || cls == C_BCFLUID_OUTER);
     double fin[4] = {0.0, 0.0, 0.0, 0.0};
     const uint32_t tag = (w >> NW_PAYLOAD_SHIFT) & 0xFFu;
-    if (bcf) masked_momentum64(a.tag_in[tag], m, fin);
+    if (bcf) masked_momentum(a.tag_in[tag], m, fin);
     collide(m, a.omega);
     if (bcf) {
         double fo[4];
-        masked_momentum64(a.tag_out[tag], m, fo);
+        masked_momentum(a.tag_out[tag], m, fo);
         float *e = a.side + side_index(slot, x, y, z, x0, y0, a.nz, TILE_X, a.tile_y) * 16;
         e[10] = (float)(fin[0] - fo[0]);
         e[11] = (float)(fin[1] - fo[1]);

@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(128)
                 ex.mxy = ex.mxz = 0.f;
                 closure_rotated(a, nx, ny, inm, outm, ex, m);
                 double fin[4] = {0.0, 0.0, 0.0, 0.0}, fo[4];
-                if (force) masked_momentum64(inm, m, fin);
+                if (force) masked_momentum(inm, m, fin);
                 collide(m, a.omega);
                 const int64_t ai = aos_at<S>(x, y, z, a.nxb, a.ny);
                 if (kScaled<S> && a.sr_step)
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(128)
                 else
                     store_mom<S>((S *)a.m[parity ^ 1], ai, m, a.rho0, a.sc);
                 if (force) {
-                    masked_momentum64(outm, m, fo);
+                    masked_momentum(outm, m, fo);
                     const double fx = fin[0] - fo[0], fy = fin[1] - fo[1];
                     acc[wi][0] = fx;
                     acc[wi][1] = fy;
