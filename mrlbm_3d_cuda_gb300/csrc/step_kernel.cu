@@ -398,7 +398,10 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
             uint32_t wqa = 0u, wqb = 0u;
             int rqa = 0, rqb = 0;
             const unsigned row_mask = w >= 32 ? 0xffffffffu : ((1u << w) - 1u);
-            auto owner_plane = [&](const int k, const Raw<S> &cur, Raw<S> &nxt, uint32_t &wq, int &rq) {
+            // wq / rq: this parity's queue slot (the plane emitted now, refilled for k + 2); wo: the
+            // other slot, which holds the word of the plane rebuilt now
+            auto owner_plane = [&](const int k, const Raw<S> &cur, Raw<S> &nxt, uint32_t &wq, int &rq,
+                                   const uint32_t wo) {
                 float *up = up_base + k4 * G::PLANE;
                 float *flt = fl_base + k3 * G::PLANE;
                 float *dn = dn_base + (k & 1) * G::PLANE;
@@ -421,6 +424,24 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                         }
                     }
                     arrive_own<S, TY>(cur, rho0, sc, up, flt, dn, col, c0, c5, c6);
+                    if constexpr (SPECIAL) {
+                        // a solid node of an updated block in the plane rebuilt now (z = zs + k - 1,
+                        // one this segment emits) keeps its stored moments, collided (the reference
+                        // collides every node of an active block): finished here from the words
+                        // in registers, before the emit would need them reloaded
+                        if (k >= 1 && k < last && (wo & NW_CLASS_MASK) == C_SOLID && !(wo & NW_FROZEN)) {
+                            Mom m = decode_words<S>(cur, rho0, sc);
+                            const int zr = zs + k - 1;
+                            const int64_t ar = k >= 2 ? soff + zst : soff;  // soff: plane zs + k - 2
+                            if (wo & NW_STENCIL)
+                                snapshot_t<TY>(side, slot, x, y, zr, x0, y0, nz, m, rho0, 1.0f, 1.0f);
+                            collide(m, omega);
+                            if (kScaled<S> && sr_on)
+                                store_mom_sr<S>(dst, ar, m, rho0, sc, sr_key(sr_seed, x, y, zr, nx, ny));
+                            else
+                                store_mom<S>(dst, ar, m, rho0, sc);
+                        }
+                    }
                 }
                 if (k >= 2) {
                     nb_sync(1 + (k & 1), G::NTH);  // FULL(k): plane k complete, emits of k-1 done
@@ -477,16 +498,6 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                             float *pq = popbuf + (rq + __popc(bal & ((1u << tx) - 1u)));
 #pragma unroll
                             for (int q = 0; q < 27; ++q) pq[(int64_t)q * n_pop] = fw[q];
-                        } else if (SPECIAL && (wd & NW_CLASS_MASK) == C_SOLID && !(wd & NW_FROZEN)) {
-                            // solid node of an updated block: its pre-stream moments, collided
-                            // (the reference collides every node of an active block)
-                            Mom m = load_mom<S>(src, ai, rho0, sc);
-                            if (wd & NW_STENCIL) snapshot_t<TY>(side, slot, x, y, z, x0, y0, nz, m, rho0, 1.0f, 1.0f);
-                            collide(m, omega);
-                            if (kScaled<S> && sr_on)
-                                store_mom_sr<S>(dst, ai, m, rho0, sc, sr_key(sr_seed, x, y, z, nx, ny));
-                            else
-                                store_mom<S>(dst, ai, m, rho0, sc);
                         }
                     }
                     if (k + 2 <= last) nb_arrive(3 + (k & 1), G::NTH);  // DONE(k)
@@ -501,8 +512,8 @@ __global__ void __launch_bounds__(Geo<TY>::NTH, Geo<TY>::MINB)
                 k4 = (k4 + 1) & 3;
             };
             for (int k = 0; k <= last; k += 2) {
-                owner_plane(k, pa, pb, wqa, rqa);
-                if (k + 1 <= last) owner_plane(k + 1, pb, pa, wqb, rqb);
+                owner_plane(k, pa, pb, wqa, rqa, wqb);
+                if (k + 1 <= last) owner_plane(k + 1, pb, pa, wqb, rqb, wqa);
             }
             if (diag) {
                 dmD += (double)dm;

@@ -245,6 +245,26 @@ __device__ __forceinline__ void rebuild(const Raw<S> &r, float rho0, const Stora
     }
 }
 
+// Moments (full rho) of a node from its loaded words: load_mom without the load.
+template <typename S>
+__device__ __forceinline__ Mom decode_words(const Raw<S> &r, float rho0, const StorageScale &sc) {
+    float v[10];
+    if constexpr (std::is_same<S, float>::value) {
+#pragma unroll
+        for (int k = 0; k < 10; ++k) v[k] = r.v[k];
+    } else if constexpr (kHybrid<S>) {
+        hybrid_values(r.u, r.w, v);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+            const float2 t = pair_to_f<S>(r.w[j]);
+            v[2 * j] = t.x;
+            v[2 * j + 1] = t.y;
+        }
+    }
+    return decode<S>(v, rho0, sc);
+}
+
 template <typename S>
 __device__ __forceinline__ Mom load_mom(const S *__restrict__ base, int64_t ai, float rho0, const StorageScale &sc) {
     float v[10];
