@@ -370,7 +370,11 @@ int step_handle(mrlbm_handle *h, int32_t nsteps) {
             } else {
                 CK(h, launch_diag_finalize(h->d_diag_part, parts, h->d_watch, h->d_error, h->stream));
             }
-            CK(h, cudaMemcpyAsync(h->h_status, h->d_error, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+            // the early refusal of mrlbm_step reads this copy: made at the watchdog's cadence only
+            // (a step sampled in between adds no copy to the stream; mrlbm_sync reads the word
+            // itself)
+            if (h->watchdog_every > 0 && (it + 1) % h->watchdog_every == 0)
+                CK(h, cudaMemcpyAsync(h->h_status, h->d_error, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
         }
         if (h->d_sr_step) CK(h, launch_sr_tick(h->d_sr_step, h->stream));
         h->parity ^= 1;
