@@ -1,11 +1,13 @@
 // Boundary and other non-bulk nodes: one thread per listed node, after the step kernel.
 //
-// The step kernel updates every plain bulk node in its fused pass.  For a node that carries a
-// node word (domain faces / edges / corners, BCFLUID, curved-wall nodes, wall-stencil nodes)
-// it only exports the 27 pulled populations to a list-ordered buffer; this kernel applies the
-// node's closure, snapshots stencil nodes for the wall kernel, collides and stores.  Solid
-// nodes of updated blocks get no populations: the reference only collides their stored
-// moments.  Nodes of blocks the reference never updates (frozen) are in no list.
+// The step kernel updates every plain bulk node in its fused pass, including plain fluid
+// nodes whose only mark is the wall-stencil bit (it also writes their snapshot), and collides
+// the solid nodes of updated blocks in place.  For every other node that carries a node word
+// (domain faces / edges / corners, BCFLUID, BCSOLID, curved-wall nodes) it only exports the 27
+// pulled populations to a list-ordered buffer; this kernel applies the node's closure,
+// snapshots stencil nodes for the wall kernel, collides and stores.  Nodes of blocks the
+// reference never updates (frozen) are in no list.  (The C_SOLID branch below is kept for a
+// list that would carry solid nodes; the list built by the host holds none.)
 //
 // Reference (paths inside sakthi-lbm/MRLBM_3D_CUDA):
 //   evaluate_bounday_moments dispatch   MRLBM_3D/src/solver/mlbm.cu:166-184
